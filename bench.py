@@ -1,0 +1,367 @@
+"""Benchmark: segment-group integrations/s of the SimpleMOC transport sweep.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--config default|small]
+    python bench.py --impl reference ...     # the CPU reference arm
+
+A step is one power iteration of src/main.c:57-92 (transport sweep,
+renormalize_flux, update_sources, compute_keff) over the whole problem; the
+value counts N3D * S * G integrations per step.  The default workload is the
+default strawman problem (17x17 assemblies of 17x17 pins, 400 cm, 30 axial
+regions per pin, 64 azimuthal x 256 tracks, 10 polar angles, 80 stacked rays,
+50 segments per 3D track, 100 groups; ~15 GB on the device).  Inputs are
+synthetic and seeded, larger than L2 (no flush needed).
+
+`value` is the chosen mode (MIXED: the fastest mode whose FSR flux stays
+within 1e-5 of the FP64 mode); the PLAIN (reference-arithmetic) rate is
+reported beside it.  `e2e` repeats the measurement through the public C ABI
+with pinned host buffers: every step uploads all inputs, runs one power
+iteration and downloads the FSR fluxes and k_eff.
+
+With --gpus N > 1 (torchrun) every rank sweeps an independent replica of the
+problem: the sweep has no data-path collective on one problem per GPU
+("replicas only"), so scaling is weak.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+
+def _args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--config", choices=["default", "small"], default="default")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-accuracy", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0,
+                    help="target CPU time of one reference-arm sample")
+    return ap.parse_args()
+
+
+def _dist():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def _peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during a region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx = float(f[1])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": mx, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def _pinned_alloc():
+    import torch
+
+    def alloc(shape, dtype):
+        t = torch.empty(int(np.prod(shape)), dtype=getattr(torch, np.dtype(dtype).name),
+                        pin_memory=True)
+        return t.numpy().reshape(shape)
+    return alloc
+
+
+def _cpu_sample_spec(spec, target_s: float, port, threads: int):
+    """A sample of the workload for the CPU: the same sources, groups, polar
+    angles, stacked rays and segments, over fewer 2D tracks, sized to take about
+    target_s seconds of OpenMP sweep."""
+    import oracle
+    import simplemoc_gb300 as sm
+    n2d = 4
+    while True:
+        s = spec.with_(n_tracks_2d=n2d)
+        hp = sm.generate(s)
+        st = oracle.fresh_state(hp)
+        op = oracle.make_problem(hp)
+        t0 = time.perf_counter()
+        port.sweep_omp(op, st["fine_source"], st["fine_flux"], st["psi_f"], threads)
+        dt = time.perf_counter() - t0
+        if dt > 0.5 or n2d >= spec.n_tracks_2d:
+            n = int(min(spec.n_tracks_2d, max(1, n2d * target_s / max(dt, 1e-3))))
+            return spec.with_(n_tracks_2d=n)
+        n2d *= 4
+
+
+def cpu_rate(spec, target_s: float, steps: int = 1):
+    """Integrations/s of the oracle's OpenMP sweep (lock per fine region, as the
+    reference's OpenMP build) on a bounded sample of the workload."""
+    import oracle
+    import simplemoc_gb300 as sm
+    port = oracle.Port()
+    threads = port.lib.oracle_omp_max_threads()
+    sspec = _cpu_sample_spec(spec, target_s, port, threads)
+    hp = sm.generate(sspec)
+    st = oracle.fresh_state(hp)
+    op = oracle.make_problem(hp)
+    times = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        port.sweep_omp(op, st["fine_source"], st["fine_flux"], st["psi_f"], threads)
+        times.append(time.perf_counter() - t0)
+    rate = sspec.integrations_per_sweep / float(np.median(times))
+    sample = (f"OpenMP sweep of {sspec.n_tracks_2d} of {spec.n_tracks_2d} 2D tracks (all "
+              f"{spec.n_polar} polar x {spec.z_stacked} stacked 3D tracks each, "
+              f"{sspec.integrations_per_sweep:.3e} integrations) over the full source storage")
+    return rate, threads, sample, times
+
+
+def run_reference(args, spec):
+    rank, world, _ = _dist()
+    if rank != 0:
+        return
+    import oracle
+    kind = "reference" if oracle.Reference.available() else "port"
+    # warm-up + timed steps, each one bounded sample sweep
+    rate, threads, sample, times = cpu_rate(spec, args.cpu_seconds / 2,
+                                            steps=max(1, args.steps) + max(0, args.warmup))
+    timed = times[max(0, args.warmup):] or times
+    sample_ints = rate * float(np.median(times))
+    value = sample_ints / float(np.mean(timed))
+    line = {
+        "impl": "reference", "metric": "segment-group integrations/s per sweep",
+        "value": value, "unit": "integrations/s", "n_gpus": args.gpus, "steps": len(timed),
+        "warmup": args.warmup, "ms_per_step": 1e3 * float(np.mean(timed)),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded)", "config": {"workload": f"{args.config} problem",
+                                                  "sample": sample},
+        "cpu_baseline": {"value": value, "unit": "integrations/s", "cores": threads,
+                         "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": "integrations/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "note": ("the reference's own sweep code is C with a time-seeded RNG; the timed CPU "
+                 "path is the oracle's restatement of attenuate_fluxes with the reference's "
+                 "per-region OpenMP locks, pinned bit-for-bit to the reference objects in "
+                 "this repository's tests"),
+    }
+    if kind == "reference":
+        line["note"] += "; reference objects available but the sweep is timed on the port"
+    print(json.dumps(line), flush=True)
+
+
+def _traffic_from_profiles():
+    """Per-launch DRAM bytes of the sweep kernel from the committed ncu summary."""
+    p = ROOT / "profiles" / "sweep_default_traffic.txt"
+    if not p.exists():
+        return None
+    for ln in p.read_text().splitlines():
+        if ln.startswith("dram_bytes_per_launch_full_size"):
+            try:
+                return float(ln.split("=")[1].split()[0])
+            except (IndexError, ValueError):
+                return None
+    return None
+
+
+def main():
+    args = _args()
+    import simplemoc_gb300 as sm
+    spec = sm.CONFIGS[args.config]
+    if args.impl == "reference":
+        run_reference(args, spec)
+        return
+    rank, world, local = _dist()
+    import torch
+    torch.cuda.set_device(local)
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+        pg = dist
+
+    def barrier():
+        if pg:
+            pg.barrier()
+        torch.cuda.synchronize()
+
+    e2e_on = not args.no_e2e
+    alloc = _pinned_alloc() if e2e_on else None
+    hp = sm.generate(spec, with_state=e2e_on, alloc=alloc)
+    solver = sm.Solver(hp, device=local, mode="mixed")
+    K, W = max(1, args.steps), max(0, args.warmup)
+    ints = spec.integrations_per_sweep
+
+    # ---- chosen (MIXED) ------------------------------------------------------
+    if W:
+        solver.time_power_iterations(W)
+    barrier()
+    l0 = solver.launch_count()
+    with ClockSampler(local) as clk:
+        r = solver.time_power_iterations(K)
+    launches = solver.launch_count() - l0
+    barrier()
+    ms = r["ms_total"]
+    if pg:
+        t = torch.tensor([ms], device="cuda")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * ints * K / (ms / 1e3)
+    sweep_ms = r["ms_sweeps"] / K
+
+    # ---- plain (reference arithmetic) ------------------------------------------
+    solver.set_mode("plain")
+    solver.time_power_iterations(1)
+    rp = solver.time_power_iterations(K)
+    plain_value = ints * K / (rp["ms_total"] / 1e3)
+    plain_sweep_ms = rp["ms_sweeps"] / K
+    solver.set_mode("mixed")
+
+    # ---- end to end through the C ABI with host buffers ------------------------
+    e2e = None
+    if e2e_on:
+        out = {"fine_flux": alloc((spec.n_fsr * spec.n_groups,), np.float32)}
+        steps = min(K, 3)
+        solver.upload(hp)
+        solver.power_iteration(1.0)
+        solver.download(fine_flux=True, fine_source=False, psi_f=False, out=out)
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            solver.upload(hp)
+            solver.power_iteration(1.0)
+            solver.download(fine_flux=True, fine_source=False, psi_f=False, out=out)
+        dt = time.perf_counter() - t0
+        barrier()
+        e2e = {"value": world * ints * steps / dt, "unit": "integrations/s",
+               "h2d_bytes_per_step": hp.input_nbytes(),
+               "d2h_bytes_per_step": int(out["fine_flux"].nbytes + 16)}
+
+    # ---- accuracy of the chosen mode against FP64 on a reduced problem ---------
+    accuracy = None
+    if not args.no_accuracy and rank == 0:
+        aspec = spec.with_(n_tracks_2d=max(64, spec.n_tracks_2d // 64))
+        ahp = sm.generate(aspec)
+        with sm.Solver(ahp, device=local, mode="fp64") as s64, \
+                sm.Solver(ahp, device=local, mode="mixed") as smx, \
+                sm.Solver(ahp, device=local, mode="plain") as spl:
+            h64 = s64.run(3)
+            hmx = smx.run(3)
+            hpl = spl.run(3)
+            p64 = s64.download64(fine_flux=True)["fine_flux"]
+            pmx = smx.download(fine_flux=True, fine_source=False, psi_f=False)["fine_flux"]
+            ppl = spl.download(fine_flux=True, fine_source=False, psi_f=False)["fine_flux"]
+        den = np.abs(p64).max()
+        accuracy = {
+            "sample": f"{aspec.n_tracks_2d} of {spec.n_tracks_2d} 2D tracks, 3 power iterations",
+            "mixed_phi_rel_err_vs_fp64": float(np.abs(pmx - p64).max() / den),
+            "mixed_keff_rel_err_vs_fp64": abs(hmx[-1][0] - h64[-1][0]) / abs(h64[-1][0]),
+            "plain_phi_rel_err_vs_fp64": float(np.abs(ppl - p64).max() / den),
+            "plain_keff_rel_err_vs_fp64": abs(hpl[-1][0] - h64[-1][0]) / abs(h64[-1][0]),
+        }
+
+    # ---- CPU baseline (rank 0, N = 1 only) -------------------------------------
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        rate, threads, sample, _ = cpu_rate(spec, args.cpu_seconds)
+        cpu = {"value": rate, "unit": "integrations/s", "cores": threads, "kind": "port",
+               "sample": sample}
+
+    peak, peak_kind = _peaks()
+    alg_bytes = spec.algorithmic_bytes()
+    achieved = alg_bytes / (sweep_ms / 1e3) / 1e9
+    traffic = _traffic_from_profiles()
+    if rank == 0:
+        line = {
+            "metric": "segment-group integrations/s per sweep, chosen vs plain @ FSR flux rel "
+                      "err <=1e-5",
+            "value": value, "unit": "integrations/s", "n_gpus": world, "steps": K, "warmup": W,
+            "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {"workload": f"{args.config} problem: {spec.n_tracks_3d} 3D tracks x "
+                                   f"{spec.n_seg} segments x {spec.n_groups} groups, "
+                                   f"{spec.n_fsr} FSRs",
+                       "mode": "mixed", "step": "one power iteration",
+                       "l2": "inputs larger than L2 (no flush)",
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "plain": {"value": plain_value, "unit": "integrations/s",
+                      "sweep_ms": plain_sweep_ms},
+            "chosen_vs_plain": value / world / plain_value,
+            "sweep_ms": sweep_ms, "keff": r["keff"],
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "peak_source": peak_kind,
+                         "algorithmic_bytes_per_launch": alg_bytes},
+            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+            "clocks": clk.summary(), "accuracy": accuracy,
+        }
+        print(json.dumps(line), flush=True)
+    solver.close()
+    if pg:
+        pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

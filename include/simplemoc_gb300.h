@@ -1,0 +1,198 @@
+/*
+ * simplemoc_gb300.h -- C ABI of the GB300 transport-sweep library
+ * (libsimplemoc_gb300.so).
+ *
+ * The library replaces the solver layer of SimpleMOC (src/solver.c) and the
+ * track / source storage it reads (src/tracks.c, src/source.c) with device
+ * resident storage and hand-written sm_103a kernels.  Every entry point takes
+ * plain pointers and sizes and returns an int status (MOC_OK == 0); the
+ * library never calls exit().  One problem handle is driven from one host
+ * thread on one CUDA stream, like the reference's single-threaded driver.
+ *
+ * Storage model (flat, row-major, group index fastest):
+ *   2D tracks      N2D, each with S segments          seg_len[N2D*S]
+ *   3D tracks      N3D = N2D*P*Z, index (i*P + j)*Z + k (src/tracks.c:100-101)
+ *   3D segments    seg_src[N3D*S]: source region of segment n of track t
+ *   sources        NS regions, F fine axial intervals each; an FSR is (s, f)
+ *   fine_source    [NS*F*G]  (src/source.c:137 row stride G)
+ *   fine_flux      [NS*F*G]  (src/source.c:146)
+ *   sigma_t table  [n_sigt*G], row src_sigt[s] for source s
+ *   xs table       [n_xs*G*3] = (nu*SigmaF, SigmaA, chi)  (src/source.c:53-55)
+ *   scatter table  [n_xs*G*G], row g = destination group  (src/solver.c:1279)
+ *   psi_f, psi_b   [N3D*G] angular flux at the track ends (src/tracks.c:135-138)
+ */
+#ifndef SIMPLEMOC_GB300_H
+#define SIMPLEMOC_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define MOC_OK               0
+#define MOC_ERR_ARG          1  /* invalid argument or inconsistent sizes      */
+#define MOC_ERR_CUDA         2  /* a CUDA runtime call failed                  */
+#define MOC_ERR_OOM          3  /* device allocation failed                    */
+#define MOC_ERR_STATE        4  /* call out of order / handle not usable       */
+#define MOC_ERR_TIMEOUT      5  /* a bounded device wait gave up               */
+#define MOC_ERR_UNSUPPORTED  6  /* mode or size not supported by this build    */
+#define MOC_ERR_NO_DEVICE    7  /* no CUDA device visible                      */
+
+/* ---- sweep arithmetic modes (moc_set_mode) ----------------------------- */
+/* PLAIN: the reference arithmetic of attenuate_fluxes (src/solver.c:14-280)
+ * and attenuate_FSR_fluxes (src/solver.c:1040-1138) operation by operation in
+ * FP32 with the reference interpolation table (src/solver.c:1441-1464); the
+ * angular flux of every track is bit-identical to the reference's. */
+#define MOC_MODE_PLAIN   0
+/* MIXED: FP32 attenuation with fused multiply-adds, precomputed reciprocals
+ * and an accurate 1-exp(-tau) (SFU exponential plus a series below a cut-off);
+ * FP64 reductions.  Errors are stated against the FP64 mode. */
+#define MOC_MODE_MIXED   1
+/* FP64: the same formulas in double precision with exact 1-exp(-tau); the
+ * high-precision yardstick for MIXED at sizes a CPU cannot sweep. */
+#define MOC_MODE_FP64    2
+
+/* mode flags */
+#define MOC_FLAG_COMPENSATED 0x1  /* MIXED: compensated (hi/lo) FSR tallies  */
+
+/* ---- problem description ---------------------------------------------- */
+typedef struct moc_dims {
+  int32_t n_groups;      /* G   Input.n_egroups                              */
+  int32_t fai;           /* F   fine axial intervals per coarse interval     */
+  int32_t cai;           /*     coarse axial intervals                        */
+  int32_t decomp_ax;     /*     Input.decomp_assemblies_ax                    */
+  float   height;        /*     Input.height                                  */
+  int32_t axial_exp;     /*     2 = quadratic source, 0 = flat source         */
+  int64_t n_sources;     /* NS  Input.n_source_regions_per_node              */
+  int32_t n_sigt;        /*     rows of the sigma_t table                     */
+  int32_t n_xs;          /*     rows of the xs / scatter tables               */
+  int64_t n_tracks_2d;   /* N2D Input.ntracks_2D                              */
+  int32_t n_polar;       /* P   Input.n_polar_angles                          */
+  int32_t z_stacked;     /* Z   Input.z_stacked                               */
+  int32_t n_seg;         /* S   segments per 3D track                         */
+  int32_t table_n;       /*     exponential table intervals (Table.N)         */
+  float   table_dx;      /*     Table.dx                                      */
+  float   table_maxval;  /*     Table.maxVal (already reduced by dx)          */
+} moc_dims;
+
+typedef struct moc_host {
+  const float   *seg_len;      /* [N2D*S]    2D segment lengths               */
+  const int32_t *seg_src;      /* [N3D*S]    source region of each 3D segment */
+  const float   *az_weight;    /* [N2D]      Track2D.az_weight                */
+  const float   *p_weight;     /* [N3D]      Track.p_weight                   */
+  const float   *z0;           /* [N3D]      Track.z_height at sweep start    */
+  const float   *polar_angles; /* [P]        Params.polar_angles              */
+  const int32_t *src_sigt;     /* [NS]       sigma_t row of each source       */
+  const int32_t *src_xs;       /* [NS]       xs / scatter row of each source  */
+  const float   *vol;          /* [NS]       Source.vol                       */
+  const float   *sigt;         /* [n_sigt*G]                                  */
+  const float   *xs;           /* [n_xs*G*3]                                  */
+  const float   *scatter;      /* [n_xs*G*G]                                  */
+  const float   *fine_source;  /* [NS*F*G]                                    */
+  const float   *fine_flux;    /* [NS*F*G]   NULL = zeros                     */
+  const float   *psi_f;        /* [N3D*G]    NULL = zeros                     */
+  const float   *psi_b;        /* [N3D*G]    NULL = zeros                     */
+  const float   *table;        /* [2*table_n] (slope, intercept) pairs        */
+} moc_host;
+
+typedef struct moc_problem moc_problem;   /* opaque device-side problem */
+
+/* ---- exponential table (host) ------------------------------------------ */
+/* Number of intervals buildExponentialTable uses (src/utils.c:54). */
+int32_t moc_exp_table_size(float precision, float maxval);
+/* Fills values[2*N] exactly as buildExponentialTable (src/utils.c:48-78),
+ * and the derived dx and reduced maxVal. */
+int moc_build_exp_table(float precision, float maxval, float *values,
+                        int32_t n, float *dx_out, float *maxval_out);
+
+/* ---- synthetic problem generator (host, seeded, counter-based) ---------- */
+typedef struct moc_gen_params {
+  uint64_t seed;
+  int32_t  n_materials;     /* rows of every cross-section table (8)          */
+  int32_t  n_fuel;          /* materials < n_fuel carry nu*SigmaF (4)          */
+  float    len_lo, len_hi;  /* 2D segment length range (0.05, 1.5) cm         */
+  float    sigt_lo, sigt_hi;/* sigma_t range (0.1, 2.0) /cm                   */
+  float    scatter_ratio;   /* scatter row sum (0.7)                           */
+  float    nusf_hi;         /* nu*SigmaF ~ U(0, nusf_hi) in fuel (0.05)        */
+  float    siga_ratio;      /* SigmaA = siga_ratio * sigma_t (0.3)             */
+  float    vol_lo, vol_hi;  /* source volume range (0.5, 1.5)                 */
+  float    axial_z_sep;     /* stacked-ray spacing; 0 = height / Z            */
+} moc_gen_params;
+
+/* Fills every array of `out` (caller-allocated with the sizes given by
+ * `dims`; psi and fine_flux may be NULL and are then left alone).  Values
+ * depend only on (seed, array, index), never on the thread count. */
+int moc_generate(const moc_dims *dims, const moc_gen_params *gp,
+                 float *seg_len, int32_t *seg_src, float *az_weight,
+                 float *p_weight, float *z0, float *polar_angles,
+                 int32_t *src_sigt, int32_t *src_xs, float *vol, float *sigt,
+                 float *xs, float *scatter, float *fine_source);
+
+/* ---- device problem lifecycle ------------------------------------------ */
+/* Replaces the one-time setup of build_tracks (src/init.c:106-159) on the
+ * device: allocates device storage for `dims` and uploads `host`. */
+int moc_create(const moc_dims *dims, const moc_host *host, int device,
+               moc_problem **out);
+int moc_destroy(moc_problem *p);
+/* Re-uploads every input array of `host` into the existing storage (same
+ * dims).  Used to time the host-to-device leg of a full call sequence. */
+int moc_upload(moc_problem *p, const moc_host *host);
+/* Copies results back (any pointer may be NULL to skip that array). */
+int moc_download(moc_problem *p, float *fine_flux, float *fine_source,
+                 float *psi_f, float *psi_b);
+/* FP64 state (valid after moc_set_mode(MOC_MODE_FP64)); NULL skips. */
+int moc_download64(moc_problem *p, double *fine_flux, double *fine_source,
+                   double *psi_f, double *psi_b);
+/* Sticky error status of the handle (first failure since create). */
+int moc_status(const moc_problem *p);
+const char *moc_status_string(int status);
+/* Device bytes held by the handle. */
+int64_t moc_device_bytes(const moc_problem *p);
+
+/* ---- modes and launch shape -------------------------------------------- */
+int moc_set_mode(moc_problem *p, int mode, int flags);
+/* Threads per track (4, 8, 16 or 32) and 4-group chunks per thread (1, 2, 4)
+ * for the sweep kernel; 0, 0 = pick automatically (autotuner choice). */
+int moc_set_launch(moc_problem *p, int threads_per_track, int chunks_per_thread);
+int moc_get_launch(const moc_problem *p, int *threads_per_track,
+                   int *chunks_per_thread);
+
+/* ---- the hot path (replaces src/solver.c) ------------------------------- */
+/* transport_sweep (src/solver.c:283-552) over the explicit 3D tracks:
+ * attenuates every segment, tallies fine_flux, updates psi_f in place.
+ * *segments_processed = N3D*S (Input.segments_processed, solver.c:549). */
+int moc_transport_sweep(moc_problem *p, int64_t *segments_processed);
+/* renormalize_flux (src/solver.c:1143-1230), FP64 fission-rate sum. */
+int moc_renormalize_flux(moc_problem *p);
+/* update_sources (src/solver.c:1235-1320); returns the source residual. */
+int moc_update_sources(moc_problem *p, double keff, double *residual);
+/* compute_keff (src/solver.c:1324-1437); leakage as Params.leakage. */
+int moc_compute_keff(moc_problem *p, double leakage, double *keff);
+/* One power iteration of src/main.c:57-92 (sweep, renormalize, update with
+ * keff_in, compute keff). */
+int moc_power_iteration(moc_problem *p, double keff_in, double *keff_out,
+                        double *residual);
+/* Waits for the handle's stream. */
+int moc_synchronize(moc_problem *p);
+
+/* ---- timing helpers (CUDA events on the handle's stream) --------------- */
+/* Runs `iters` sweeps and returns the mean device time of one sweep kernel
+ * launch in milliseconds, measured with events on the launching stream. */
+int moc_time_sweep(moc_problem *p, int iters, double *ms_per_sweep);
+/* Runs `iters` power iterations back to back with k_eff kept on the device
+ * (update_sources of iteration i uses the k_eff of iteration i-1, starting
+ * from the last value computed or given).  Reports the device time of the
+ * whole sequence and of the sweep kernels alone (both from events on the
+ * launching stream) and the final k_eff and residual. */
+int moc_time_power_iterations(moc_problem *p, int iters, double *ms_total,
+                              double *ms_sweeps, double *keff, double *residual);
+/* Number of kernels the library has launched on this handle so far. */
+int64_t moc_launch_count(const moc_problem *p);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SIMPLEMOC_GB300_H */

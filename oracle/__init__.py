@@ -1,0 +1,258 @@
+"""Python binding of the CPU oracle -- TEST INFRASTRUCTURE ONLY.
+
+Only tests/, __graft_entry__.smoke() and the CPU-baseline legs of bench.py may
+import this package; the product never does.  Two libraries:
+
+  port       oracle/_build/libmoc_oracle.so: the C restatement (moc_oracle.c)
+  reference  oracle/_ref/libref_harness.so: the reference's own solver objects
+             driven over the same explicit segment streams (built only where the
+             reference sources are mounted)
+
+Problems are passed duck-typed: any object with the array attributes of
+simplemoc_gb300.problem.HostProblem (numpy, C-contiguous).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+PORT_LIB = HERE / "_build" / "libmoc_oracle.so"
+REF_LIB = HERE / "_ref" / "libref_harness.so"
+REF_SRC = Path(os.environ.get("SIMPLEMOC_REF_SRC", "/root/reference/src"))
+
+f32p = C.POINTER(C.c_float)
+f64p = C.POINTER(C.c_double)
+i32p = C.POINTER(C.c_int32)
+i64p = C.POINTER(C.c_int64)
+
+
+class OracleProblem(C.Structure):
+    _fields_ = [
+        ("G", C.c_int32), ("F", C.c_int32), ("cai", C.c_int32), ("decomp_ax", C.c_int32),
+        ("height", C.c_float), ("axial_exp", C.c_int32), ("NS", C.c_int64), ("N2D", C.c_int64),
+        ("P", C.c_int32), ("Z", C.c_int32), ("S", C.c_int32),
+        ("seg_len", f32p), ("seg_src", i32p), ("az_weight", f32p), ("p_weight", f32p),
+        ("z0", f32p), ("polar_angles", f32p), ("src_sigt", i32p), ("src_xs", i32p),
+        ("vol", f32p), ("sigt", f32p), ("xs", f32p), ("scatter", f32p), ("table", f32p),
+        ("table_n", C.c_int32), ("table_dx", C.c_float), ("table_maxval", C.c_float),
+    ]
+
+
+def build(reference: bool | None = None) -> None:
+    """make -C oracle port [ref]; `ref` only where the reference sources exist."""
+    targets = ["port"]
+    if reference is None:
+        reference = (REF_SRC / "solver.c").exists()
+    if reference:
+        targets.append("ref")
+    subprocess.run(["make", "-s", "-C", str(HERE), f"REF_SRC={REF_SRC}", *targets], check=True,
+                   capture_output=True)
+
+
+def _p(a, t):
+    if a is None:
+        return None
+    assert a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(C.POINTER(t))
+
+
+def make_problem(hp) -> OracleProblem:
+    s = hp.spec
+    op = OracleProblem(
+        G=s.n_groups, F=s.fai, cai=s.cai, decomp_ax=s.decomp_ax, height=s.height,
+        axial_exp=s.axial_exp, NS=s.n_sources, N2D=s.n_tracks_2d, P=s.n_polar, Z=s.z_stacked,
+        S=s.n_seg, seg_len=_p(hp.seg_len, C.c_float), seg_src=_p(hp.seg_src, C.c_int32),
+        az_weight=_p(hp.az_weight, C.c_float), p_weight=_p(hp.p_weight, C.c_float),
+        z0=_p(hp.z0, C.c_float), polar_angles=_p(hp.polar_angles, C.c_float),
+        src_sigt=_p(hp.src_sigt, C.c_int32), src_xs=_p(hp.src_xs, C.c_int32),
+        vol=_p(hp.vol, C.c_float), sigt=_p(hp.sigt, C.c_float), xs=_p(hp.xs, C.c_float),
+        scatter=_p(hp.scatter, C.c_float), table=_p(hp.table, C.c_float),
+        table_n=hp.table_n, table_dx=hp.table_dx, table_maxval=hp.table_maxval)
+    op._keep = hp          # arrays must outlive the struct
+    return op
+
+
+class Port:
+    """The C restatement (moc_oracle.c)."""
+
+    def __init__(self, path: Path = PORT_LIB):
+        if not path.exists():
+            build(reference=False)
+        lib = C.CDLL(str(path))
+        P = C.POINTER(OracleProblem)
+        sig = {
+            "oracle_exp_table_size": (C.c_int32, [C.c_float, C.c_float]),
+            "oracle_build_exp_table": (None, [C.c_float, C.c_float, f32p, f32p, f32p,
+                                              C.POINTER(C.c_int32)]),
+            "oracle_interpolate": (C.c_float, [f32p, C.c_float, C.c_float, C.c_float]),
+            "oracle_pairwise_sum": (C.c_float, [f32p, C.c_int64]),
+            "oracle_sweep": (C.c_int64, [P, f32p, f32p, f32p]),
+            "oracle_sweep_tracks": (None, [P, f32p, i64p, C.c_int64, f32p, f32p, f32p]),
+            "oracle_sweep_omp": (C.c_int64, [P, f32p, f32p, f32p, C.c_int]),
+            "oracle_omp_max_threads": (C.c_int, []),
+            "oracle_renormalize": (None, [P, f32p, f32p, f32p]),
+            "oracle_update_sources": (C.c_float, [P, f32p, f32p, C.c_float]),
+            "oracle_compute_keff": (C.c_float, [P, f32p, C.c_float]),
+            "oracle_sweep64": (C.c_int64, [P, f64p, f64p, f64p]),
+            "oracle_renormalize64": (None, [P, f64p, f64p, f64p]),
+            "oracle_update_sources64": (C.c_double, [P, f64p, f64p, C.c_double]),
+            "oracle_compute_keff64": (C.c_double, [P, f64p, C.c_double]),
+        }
+        for n, (r, a) in sig.items():
+            fn = getattr(lib, n)
+            fn.restype = r
+            fn.argtypes = a
+        self.lib = lib
+
+    def exp_table(self, precision: float, maxval: float = 10.0):
+        n = self.lib.oracle_exp_table_size(precision, maxval)
+        vals = np.empty(2 * n, dtype=np.float32)
+        dx, mv, nn = C.c_float(), C.c_float(), C.c_int32()
+        self.lib.oracle_build_exp_table(precision, maxval, _p(vals, C.c_float), C.byref(dx),
+                                        C.byref(mv), C.byref(nn))
+        return vals, dx.value, mv.value, nn.value
+
+    def sweep(self, op, q, phi, psi_f) -> int:
+        f = C.c_float
+        return self.lib.oracle_sweep(C.byref(op), _p(q, f), _p(phi, f), _p(psi_f, f))
+
+    def sweep_omp(self, op, q, phi, psi_f, nthreads: int = 0) -> int:
+        f = C.c_float
+        return self.lib.oracle_sweep_omp(C.byref(op), _p(q, f), _p(phi, f), _p(psi_f, f),
+                                         nthreads)
+
+    def sweep_tracks(self, op, q, tracks, psi_in, phi=None):
+        G = op.G
+        tracks = np.ascontiguousarray(tracks, dtype=np.int64)
+        out = np.empty(len(tracks) * G, dtype=np.float32)
+        f = C.c_float
+        self.lib.oracle_sweep_tracks(C.byref(op), _p(q, f), _p(tracks, C.c_int64), len(tracks),
+                                     _p(psi_in, f), _p(out, f), _p(phi, f))
+        return out
+
+    def renormalize(self, op, phi, psi_f, psi_b) -> None:
+        f = C.c_float
+        self.lib.oracle_renormalize(C.byref(op), _p(phi, f), _p(psi_f, f), _p(psi_b, f))
+
+    def update_sources(self, op, phi, q, keff: float) -> float:
+        f = C.c_float
+        return self.lib.oracle_update_sources(C.byref(op), _p(phi, f), _p(q, f), keff)
+
+    def compute_keff(self, op, phi, leakage: float = 0.0) -> float:
+        return self.lib.oracle_compute_keff(C.byref(op), _p(phi, C.c_float), leakage)
+
+    def sweep64(self, op, q, phi, psi_f) -> int:
+        d = C.c_double
+        return self.lib.oracle_sweep64(C.byref(op), _p(q, d), _p(phi, d), _p(psi_f, d))
+
+    def renormalize64(self, op, phi, psi_f, psi_b) -> None:
+        d = C.c_double
+        self.lib.oracle_renormalize64(C.byref(op), _p(phi, d), _p(psi_f, d), _p(psi_b, d))
+
+    def update_sources64(self, op, phi, q, keff: float) -> float:
+        d = C.c_double
+        return self.lib.oracle_update_sources64(C.byref(op), _p(phi, d), _p(q, d), keff)
+
+    def compute_keff64(self, op, phi, leakage: float = 0.0) -> float:
+        return self.lib.oracle_compute_keff64(C.byref(op), _p(phi, C.c_double), leakage)
+
+    # -- a whole power iteration (src/main.c:57-92) ---------------------------
+    def iterate(self, hp, state: dict, n_iters: int, keff: float = 1.0, threads: int = 1):
+        """state: dict with fine_source, fine_flux, psi_f, psi_b (float32, updated)."""
+        op = make_problem(hp)
+        hist = []
+        for _ in range(n_iters):
+            if threads == 1:
+                self.sweep(op, state["fine_source"], state["fine_flux"], state["psi_f"])
+            else:
+                self.sweep_omp(op, state["fine_source"], state["fine_flux"], state["psi_f"],
+                               threads)
+            self.renormalize(op, state["fine_flux"], state["psi_f"], state["psi_b"])
+            res = self.update_sources(op, state["fine_flux"], state["fine_source"], keff)
+            keff = self.compute_keff(op, state["fine_flux"], 0.0)
+            hist.append((float(keff), float(res)))
+        return hist
+
+    def iterate64(self, hp, state: dict, n_iters: int, keff: float = 1.0):
+        op = make_problem(hp)
+        hist = []
+        for _ in range(n_iters):
+            self.sweep64(op, state["fine_source"], state["fine_flux"], state["psi_f"])
+            self.renormalize64(op, state["fine_flux"], state["psi_f"], state["psi_b"])
+            res = self.update_sources64(op, state["fine_flux"], state["fine_source"], keff)
+            keff = self.compute_keff64(op, state["fine_flux"], 0.0)
+            hist.append((float(keff), float(res)))
+        return hist
+
+
+class Reference:
+    """The reference's own compiled solver (oracle/_ref), if it was built here."""
+
+    def __init__(self, path: Path = REF_LIB):
+        if not path.exists():
+            raise FileNotFoundError(f"{path} not built (needs the reference sources)")
+        lib = C.CDLL(str(path))
+        P = C.POINTER(OracleProblem)
+        sig = {
+            "refh_setup": (C.c_int, [P, C.c_float, f32p, f32p, f32p, f32p]),
+            "refh_sweep": (C.c_long, []),
+            "refh_renormalize": (None, []),
+            "refh_update_sources": (C.c_float, [C.c_float]),
+            "refh_compute_keff": (C.c_float, []),
+            "refh_table": (C.c_int, [C.c_float, f32p, C.c_int, f32p, f32p]),
+            "refh_teardown": (None, []),
+        }
+        for n, (r, a) in sig.items():
+            fn = getattr(lib, n)
+            fn.restype = r
+            fn.argtypes = a
+        self.lib = lib
+
+    @staticmethod
+    def available() -> bool:
+        return REF_LIB.exists()
+
+    def exp_table(self, precision: float):
+        cap = 1 << 20
+        vals = np.empty(2 * cap, dtype=np.float32)
+        dx, mv = C.c_float(), C.c_float()
+        n = self.lib.refh_table(precision, _p(vals, C.c_float), cap, C.byref(dx), C.byref(mv))
+        return vals[:2 * n].copy(), dx.value, mv.value, n
+
+    def iterate(self, hp, state: dict, n_iters: int, keff: float = 1.0, sweep_only=False):
+        op = make_problem(hp)
+        f = C.c_float
+        self.lib.refh_setup(C.byref(op), hp.spec.precision, _p(state["fine_source"], f),
+                            _p(state["fine_flux"], f), _p(state["psi_f"], f),
+                            _p(state["psi_b"], f))
+        hist = []
+        try:
+            for _ in range(n_iters):
+                self.lib.refh_sweep()
+                if sweep_only:
+                    continue
+                self.lib.refh_renormalize()
+                res = self.lib.refh_update_sources(keff)
+                keff = self.lib.refh_compute_keff()
+                hist.append((float(keff), float(res)))
+        finally:
+            self.lib.refh_teardown()
+        return hist
+
+
+def fresh_state(hp, dtype=np.float32) -> dict:
+    s = hp.spec
+    nf, nt = s.n_fsr * s.n_groups, s.n_tracks_3d * s.n_groups
+    st = {
+        "fine_source": hp.fine_source.astype(dtype, copy=True),
+        "fine_flux": (np.zeros(nf, dtype) if hp.fine_flux is None
+                      else hp.fine_flux.astype(dtype, copy=True)),
+        "psi_f": np.zeros(nt, dtype) if hp.psi_f is None else hp.psi_f.astype(dtype, copy=True),
+        "psi_b": np.zeros(nt, dtype) if hp.psi_b is None else hp.psi_b.astype(dtype, copy=True),
+    }
+    return st

@@ -1,0 +1,526 @@
+// moc_api.cu -- the C ABI of libsimplemoc_gb300.so: problem lifecycle,
+// uploads and downloads, modes, and the four solver entry points of
+// src/solver.c (transport_sweep, renormalize_flux, update_sources,
+// compute_keff) over device-resident storage.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string.h>
+
+#include <new>
+#include <vector>
+
+#include "moc_host.h"
+#include "moc_internal.h"
+
+namespace {
+
+__global__ void widen_kernel(const float *__restrict__ src, double *__restrict__ dst, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    dst[i] = (double)src[i];
+}
+
+__global__ void fold_kernel(float *__restrict__ hi, float *__restrict__ lo, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    hi[i] = hi[i] + lo[i];
+    lo[i] = 0.0f;
+  }
+}
+
+template <typename T>
+int dalloc(moc_problem *p, T **ptr, int64_t count) {
+  if (count <= 0) count = 1;
+  void *d = nullptr;
+  cudaError_t e = cudaMalloc(&d, sizeof(T) * (size_t)count);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return e == cudaErrorMemoryAllocation ? MOC_ERR_OOM : MOC_ERR_CUDA;
+  }
+  *ptr = static_cast<T *>(d);
+  p->bytes += (int64_t)sizeof(T) * count;
+  return MOC_OK;
+}
+
+template <typename T>
+void dfree(T *&ptr) {
+  if (ptr) cudaFree(ptr);
+  ptr = nullptr;
+}
+
+// Copies a [rows x G] host matrix into a [rows x ldg] device matrix.
+int put_rows(moc_problem *p, float *dst, const float *src, int64_t rows) {
+  const int64_t G = p->d.n_groups, L = p->ldg;
+  if (!src) {
+    MOC_CUDA_TRY(cudaMemsetAsync(dst, 0, sizeof(float) * (size_t)(rows * L), p->stream));
+    return MOC_OK;
+  }
+  if (L == G) {
+    MOC_CUDA_TRY(cudaMemcpyAsync(dst, src, sizeof(float) * (size_t)(rows * G),
+                                 cudaMemcpyHostToDevice, p->stream));
+  } else {
+    MOC_CUDA_TRY(cudaMemsetAsync(dst, 0, sizeof(float) * (size_t)(rows * L), p->stream));
+    MOC_CUDA_TRY(cudaMemcpy2DAsync(dst, sizeof(float) * L, src, sizeof(float) * G,
+                                   sizeof(float) * G, (size_t)rows, cudaMemcpyHostToDevice,
+                                   p->stream));
+  }
+  return MOC_OK;
+}
+
+template <typename T>
+int get_rows(moc_problem *p, T *dst, const T *src, int64_t rows) {
+  const int64_t G = p->d.n_groups, L = p->ldg;
+  if (L == G) {
+    MOC_CUDA_TRY(cudaMemcpyAsync(dst, src, sizeof(T) * (size_t)(rows * G), cudaMemcpyDeviceToHost,
+                                 p->stream));
+  } else {
+    MOC_CUDA_TRY(cudaMemcpy2DAsync(dst, sizeof(T) * G, src, sizeof(T) * L, sizeof(T) * G,
+                                   (size_t)rows, cudaMemcpyDeviceToHost, p->stream));
+  }
+  return MOC_OK;
+}
+
+template <typename T>
+int put(moc_problem *p, T *dst, const T *src, int64_t count) {
+  MOC_CUDA_TRY(
+      cudaMemcpyAsync(dst, src, sizeof(T) * (size_t)count, cudaMemcpyHostToDevice, p->stream));
+  return MOC_OK;
+}
+
+#define TRY(x)                      \
+  do {                              \
+    int rc_ = (x);                  \
+    if (rc_ != MOC_OK) return rc_;  \
+  } while (0)
+
+// Uploads every input and state array of `h` (validated) into the storage.
+int upload_all(moc_problem *p, const moc_host *h) {
+  const moc_dims &d = p->d;
+  const int64_t N2D = d.n_tracks_2d, P = d.n_polar, S = d.n_seg, G = d.n_groups;
+  const int64_t NS = d.n_sources;
+  std::vector<float> seg_ds((size_t)(N2D * P * S)), mu((size_t)P), weight((size_t)p->n3d);
+  std::vector<float> coef((size_t)d.n_sigt * COEF_PLANES * p->ldg);
+  std::vector<float> st((size_t)d.n_xs * G * G);
+  float max_step = 0.0f;
+  TRY(moc_host_derive(&d, h, p->ldg, seg_ds.data(), mu.data(), weight.data(), coef.data(),
+                      st.data(), &max_step));
+  // one wrap per segment keeps the height rule exact (checked, not assumed)
+  const float hd = d.height / (float)d.decomp_ax;
+  if (!(max_step < hd)) return MOC_ERR_ARG;
+  TRY(put(p, p->seg_ds, seg_ds.data(), N2D * P * S));
+  TRY(put(p, p->seg_src, h->seg_src, p->n3d * S));
+  TRY(put(p, p->weight, weight.data(), p->n3d));
+  TRY(put(p, p->z0, h->z0, p->n3d));
+  TRY(put(p, p->mu, mu.data(), P));
+  TRY(put(p, p->src_sigt, h->src_sigt, NS));
+  TRY(put(p, p->src_xs, h->src_xs, NS));
+  TRY(put(p, p->vol, h->vol, NS));
+  TRY(put(p, p->coef, coef.data(), (int64_t)coef.size()));
+  TRY(put(p, p->xs, h->xs, (int64_t)d.n_xs * G * 3));
+  TRY(put(p, p->scatter_t, st.data(), (int64_t)st.size()));
+  TRY(put(p, p->table, h->table, 2 * (int64_t)d.table_n));
+  TRY(put_rows(p, p->q, h->fine_source, p->nfsr));
+  TRY(put_rows(p, p->phi, h->fine_flux, p->nfsr));
+  TRY(put_rows(p, p->psi_f, h->psi_f, p->n3d));
+  TRY(put_rows(p, p->psi_b, h->psi_b, p->n3d));
+  if (p->phi_lo)
+    MOC_CUDA_TRY(cudaMemsetAsync(p->phi_lo, 0, sizeof(float) * (size_t)(p->nfsr * p->ldg), p->stream));
+  // fresh FP64 state follows the uploaded FP32 state
+  if (p->q64) {
+    widen_kernel<<<1024, 256, 0, p->stream>>>(p->q, p->q64, p->nfsr * p->ldg);
+    widen_kernel<<<1024, 256, 0, p->stream>>>(p->phi, p->phi64, p->nfsr * p->ldg);
+    widen_kernel<<<1024, 256, 0, p->stream>>>(p->psi_f, p->psi_f64, p->n3d * p->ldg);
+    widen_kernel<<<1024, 256, 0, p->stream>>>(p->psi_b, p->psi_b64, p->n3d * p->ldg);
+    p->launches += 4;
+  }
+  MOC_CUDA_TRY(cudaMemsetAsync(p->err, 0, sizeof(int32_t), p->stream));
+  return MOC_OK;
+}
+
+void release(moc_problem *p) {
+  dfree(p->seg_ds); dfree(p->seg_src); dfree(p->weight); dfree(p->z0); dfree(p->mu);
+  dfree(p->src_sigt); dfree(p->src_xs); dfree(p->vol); dfree(p->coef); dfree(p->xs);
+  dfree(p->scatter_t); dfree(p->table); dfree(p->q); dfree(p->phi); dfree(p->phi_lo);
+  dfree(p->psi_f); dfree(p->psi_b); dfree(p->q64); dfree(p->phi64); dfree(p->psi_f64);
+  dfree(p->psi_b64); dfree(p->partials); dfree(p->scalars); dfree(p->err);
+  if (p->ev0) cudaEventDestroy(p->ev0);
+  if (p->ev1) cudaEventDestroy(p->ev1);
+  if (p->stream) cudaStreamDestroy(p->stream);
+  p->ev0 = p->ev1 = nullptr;
+  p->stream = nullptr;
+}
+
+// Records a failure on the handle; later calls report MOC_ERR_STATE.
+int fail(moc_problem *p, int rc) {
+  if (rc != MOC_OK && p->status == MOC_OK) p->status = rc;
+  return rc;
+}
+
+int usable(const moc_problem *p) {
+  if (!p) return MOC_ERR_ARG;
+  if (p->status != MOC_OK) return MOC_ERR_STATE;
+  return MOC_OK;
+}
+
+// Waits for the stream and folds the device error word into the status.
+int sync_check(moc_problem *p) {
+  cudaError_t e = cudaStreamSynchronize(p->stream);
+  if (e != cudaSuccess) return fail(p, MOC_ERR_CUDA);
+  int32_t err = 0;
+  e = cudaMemcpy(&err, p->err, sizeof(int32_t), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return fail(p, MOC_ERR_CUDA);
+  if (err != 0) return fail(p, MOC_ERR_ARG);
+  return MOC_OK;
+}
+
+int read_scalars(moc_problem *p, double *out) {
+  int rc = sync_check(p);
+  if (rc != MOC_OK) return rc;
+  if (cudaMemcpy(out, p->scalars, sizeof(double) * SC_COUNT, cudaMemcpyDeviceToHost) != cudaSuccess)
+    return fail(p, MOC_ERR_CUDA);
+  return MOC_OK;
+}
+
+int sweep_impl(moc_problem *p) {
+  int rc = moc_launch_sweep(p);
+  if (rc != MOC_OK) return fail(p, rc);
+  if (p->mode == MOC_MODE_MIXED && (p->flags & MOC_FLAG_COMPENSATED) && p->phi_lo) {
+    fold_kernel<<<1024, 256, 0, p->stream>>>(p->phi, p->phi_lo, p->nfsr * p->ldg);
+    p->launches++;
+    if (cudaGetLastError() != cudaSuccess) return fail(p, MOC_ERR_CUDA);
+  }
+  return MOC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *moc_status_string(int status) {
+  switch (status) {
+    case MOC_OK: return "ok";
+    case MOC_ERR_ARG: return "invalid argument";
+    case MOC_ERR_CUDA: return "CUDA runtime error";
+    case MOC_ERR_OOM: return "device out of memory";
+    case MOC_ERR_STATE: return "handle unusable after an earlier error";
+    case MOC_ERR_TIMEOUT: return "bounded device wait gave up";
+    case MOC_ERR_UNSUPPORTED: return "unsupported mode or size";
+    case MOC_ERR_NO_DEVICE: return "no CUDA device";
+    default: return "unknown status";
+  }
+}
+
+int moc_create(const moc_dims *dims, const moc_host *host, int device, moc_problem **out) {
+  if (!dims || !host || !out) return MOC_ERR_ARG;
+  *out = nullptr;
+  int rc = moc_host_validate(dims, host);
+  if (rc != MOC_OK) return rc;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+    cudaGetLastError();
+    return MOC_ERR_NO_DEVICE;
+  }
+  if (device < 0 || device >= ndev) return MOC_ERR_ARG;
+  if (cudaSetDevice(device) != cudaSuccess) return MOC_ERR_CUDA;
+  moc_problem *p = new (std::nothrow) moc_problem();
+  if (!p) return MOC_ERR_OOM;
+  p->d = *dims;
+  p->device = device;
+  p->ldg = (dims->n_groups + 3) / 4 * 4;
+  p->n3d = dims->n_tracks_2d * dims->n_polar * dims->z_stacked;
+  p->nfsr = dims->n_sources * dims->fai;
+  const int64_t N2D = dims->n_tracks_2d, P = dims->n_polar, S = dims->n_seg;
+  const int64_t G = dims->n_groups, NS = dims->n_sources;
+  rc = MOC_OK;
+  if (cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&p->ev0) != cudaSuccess || cudaEventCreate(&p->ev1) != cudaSuccess)
+    rc = MOC_ERR_CUDA;
+  if (rc == MOC_OK) rc = dalloc(p, &p->seg_ds, N2D * P * S);
+  if (rc == MOC_OK) rc = dalloc(p, &p->seg_src, p->n3d * S);
+  if (rc == MOC_OK) rc = dalloc(p, &p->weight, p->n3d);
+  if (rc == MOC_OK) rc = dalloc(p, &p->z0, p->n3d);
+  if (rc == MOC_OK) rc = dalloc(p, &p->mu, P);
+  if (rc == MOC_OK) rc = dalloc(p, &p->src_sigt, NS);
+  if (rc == MOC_OK) rc = dalloc(p, &p->src_xs, NS);
+  if (rc == MOC_OK) rc = dalloc(p, &p->vol, NS);
+  if (rc == MOC_OK) rc = dalloc(p, &p->coef, (int64_t)dims->n_sigt * COEF_PLANES * p->ldg);
+  if (rc == MOC_OK) rc = dalloc(p, &p->xs, (int64_t)dims->n_xs * G * 3);
+  if (rc == MOC_OK) rc = dalloc(p, &p->scatter_t, (int64_t)dims->n_xs * G * G);
+  if (rc == MOC_OK) rc = dalloc(p, &p->table, 2 * (int64_t)dims->table_n);
+  if (rc == MOC_OK) rc = dalloc(p, &p->q, p->nfsr * p->ldg);
+  if (rc == MOC_OK) rc = dalloc(p, &p->phi, p->nfsr * p->ldg);
+  if (rc == MOC_OK) rc = dalloc(p, &p->psi_f, p->n3d * p->ldg);
+  if (rc == MOC_OK) rc = dalloc(p, &p->psi_b, p->n3d * p->ldg);
+  if (rc == MOC_OK) rc = dalloc(p, &p->partials, 3 * (int64_t)moc_post_scratch_blocks() + NS);
+  if (rc == MOC_OK) rc = dalloc(p, &p->scalars, (int64_t)SC_COUNT);
+  if (rc == MOC_OK) rc = dalloc(p, &p->err, 1);
+  if (rc == MOC_OK) {
+    double init[SC_COUNT] = {0};
+    init[SC_KEFF_IN] = 1.0;
+    init[SC_KEFF] = 1.0;
+    if (cudaMemcpy(p->scalars, init, sizeof init, cudaMemcpyHostToDevice) != cudaSuccess)
+      rc = MOC_ERR_CUDA;
+  }
+  if (rc == MOC_OK) rc = upload_all(p, host);
+  if (rc == MOC_OK && cudaStreamSynchronize(p->stream) != cudaSuccess) rc = MOC_ERR_CUDA;
+  if (rc != MOC_OK) {
+    release(p);
+    delete p;
+    return rc;
+  }
+  *out = p;
+  return MOC_OK;
+}
+
+int moc_destroy(moc_problem *p) {
+  if (!p) return MOC_ERR_ARG;
+  cudaSetDevice(p->device);
+  if (p->stream) cudaStreamSynchronize(p->stream);
+  release(p);
+  delete p;
+  return MOC_OK;
+}
+
+int moc_upload(moc_problem *p, const moc_host *host) {
+  int rc = usable(p);
+  if (rc != MOC_OK) return rc;
+  if (!host) return MOC_ERR_ARG;
+  rc = moc_host_validate(&p->d, host);
+  if (rc != MOC_OK) return rc;
+  rc = upload_all(p, host);
+  if (rc != MOC_OK) return fail(p, rc);
+  return MOC_OK;
+}
+
+int moc_download(moc_problem *p, float *fine_flux, float *fine_source, float *psi_f, float *psi_b) {
+  int rc = usable(p);
+  if (rc != MOC_OK) return rc;
+  rc = sync_check(p);
+  if (rc != MOC_OK) return rc;
+  if (fine_flux) rc = get_rows(p, fine_flux, p->phi, p->nfsr);
+  if (rc == MOC_OK && fine_source) rc = get_rows(p, fine_source, p->q, p->nfsr);
+  if (rc == MOC_OK && psi_f) rc = get_rows(p, psi_f, p->psi_f, p->n3d);
+  if (rc == MOC_OK && psi_b) rc = get_rows(p, psi_b, p->psi_b, p->n3d);
+  if (rc != MOC_OK) return fail(p, rc);
+  return sync_check(p);
+}
+
+int moc_download64(moc_problem *p, double *fine_flux, double *fine_source, double *psi_f,
+                   double *psi_b) {
+  int rc = usable(p);
+  if (rc != MOC_OK) return rc;
+  if (!p->q64) return MOC_ERR_STATE;
+  rc = sync_check(p);
+  if (rc != MOC_OK) return rc;
+  if (fine_flux) rc = get_rows(p, fine_flux, p->phi64, p->nfsr);
+  if (rc == MOC_OK && fine_source) rc = get_rows(p, fine_source, p->q64, p->nfsr);
+  if (rc == MOC_OK && psi_f) rc = get_rows(p, psi_f, p->psi_f64, p->n3d);
+  if (rc == MOC_OK && psi_b) rc = get_rows(p, psi_b, p->psi_b64, p->n3d);
+  if (rc != MOC_OK) return fail(p, rc);
+  return sync_check(p);
+}
+
+int moc_status(const moc_problem *p) { return p ? p->status : MOC_ERR_ARG; }
+
+int64_t moc_device_bytes(const moc_problem *p) { return p ? p->bytes : 0; }
+
+int64_t moc_launch_count(const moc_problem *p) { return p ? p->launches : 0; }
+
+int moc_set_mode(moc_problem *p, int mode, int flags) {
+  int rc = usable(p);
+  if (rc != MOC_OK) return rc;
+  if (mode != MOC_MODE_PLAIN && mode != MOC_MODE_MIXED && mode != MOC_MODE_FP64) return MOC_ERR_ARG;
+  if (flags & ~MOC_FLAG_COMPENSATED) return MOC_ERR_ARG;
+  if (mode == MOC_MODE_FP64 && !p->q64) {
+    // the FP64 state starts from the current FP32 state
+    rc = dalloc(p, &p->q64, p->nfsr * p->ldg);
+    if (rc == MOC_OK) rc = dalloc(p, &p->phi64, p->nfsr * p->ldg);
+    if (rc == MOC_OK) rc = dalloc(p, &p->psi_f64, p->n3d * p->ldg);
+    if (rc == MOC_OK) rc = dalloc(p, &p->psi_b64, p->n3d * p->ldg);
+    if (rc != MOC_OK) {
+      dfree(p->q64); dfree(p->phi64); dfree(p->psi_f64); dfree(p->psi_b64);
+      return rc;
+    }
+    widen_kernel<<<1024, 256, 0, p->stream>>>(p->q, p->q64, p->nfsr * p->ldg);
+    widen_kernel<<<1024, 256, 0, p->stream>>>(p->phi, p->phi64, p->nfsr * p->ldg);
+    widen_kernel<<<1024, 256, 0, p->stream>>>(p->psi_f, p->psi_f64, p->n3d * p->ldg);
+    widen_kernel<<<1024, 256, 0, p->stream>>>(p->psi_b, p->psi_b64, p->n3d * p->ldg);
+    p->launches += 4;
+    if (cudaGetLastError() != cudaSuccess) return fail(p, MOC_ERR_CUDA);
+  }
+  if (mode == MOC_MODE_MIXED && (flags & MOC_FLAG_COMPENSATED) && !p->phi_lo) {
+    rc = dalloc(p, &p->phi_lo, p->nfsr * p->ldg);
+    if (rc != MOC_OK) return rc;
+    if (cudaMemsetAsync(p->phi_lo, 0, sizeof(float) * (size_t)(p->nfsr * p->ldg), p->stream) !=
+        cudaSuccess)
+      return fail(p, MOC_ERR_CUDA);
+  }
+  p->mode = mode;
+  p->flags = flags;
+  return MOC_OK;
+}
+
+int moc_set_launch(moc_problem *p, int threads_per_track, int chunks_per_thread) {
+  if (!p) return MOC_ERR_ARG;
+  if (threads_per_track == 0 && chunks_per_thread == 0) {
+    p->tpw = p->cpl = 0;
+    return MOC_OK;
+  }
+  static const int ok[][2] = {{32, 1}, {32, 2}, {32, 4}, {16, 1}, {16, 2}, {8, 1}, {8, 4}, {4, 2}};
+  for (auto &s : ok) {
+    if (s[0] == threads_per_track && s[1] == chunks_per_thread) {
+      if ((int64_t)threads_per_track * chunks_per_thread * 4 < p->ldg) return MOC_ERR_ARG;
+      p->tpw = threads_per_track;
+      p->cpl = chunks_per_thread;
+      return MOC_OK;
+    }
+  }
+  return MOC_ERR_UNSUPPORTED;
+}
+
+int moc_get_launch(const moc_problem *p, int *threads_per_track, int *chunks_per_thread) {
+  if (!p || !threads_per_track || !chunks_per_thread) return MOC_ERR_ARG;
+  return moc_sweep_launch_shape(p, threads_per_track, chunks_per_thread);
+}
+
+int moc_transport_sweep(moc_problem *p, int64_t *segments_processed) {
+  int rc = usable(p);
+  if (rc != MOC_OK) return rc;
+  cudaSetDevice(p->device);
+  rc = sweep_impl(p);
+  if (rc != MOC_OK) return rc;
+  if (segments_processed) *segments_processed = p->n3d * p->d.n_seg;   // src/solver.c:549
+  return MOC_OK;
+}
+
+int moc_renormalize_flux(moc_problem *p) {
+  int rc = usable(p);
+  if (rc != MOC_OK) return rc;
+  cudaSetDevice(p->device);
+  rc = moc_launch_renormalize(p);
+  return rc == MOC_OK ? MOC_OK : fail(p, rc);
+}
+
+int moc_update_sources(moc_problem *p, double keff, double *residual) {
+  int rc = usable(p);
+  if (rc != MOC_OK) return rc;
+  if (!(keff != 0.0)) return MOC_ERR_ARG;
+  cudaSetDevice(p->device);
+  rc = moc_launch_update(p, keff, false, false);
+  if (rc != MOC_OK) return fail(p, rc);
+  if (residual) {
+    double sc[SC_COUNT];
+    rc = read_scalars(p, sc);
+    if (rc != MOC_OK) return rc;
+    *residual = sc[SC_RESIDUAL];
+  }
+  return MOC_OK;
+}
+
+int moc_compute_keff(moc_problem *p, double leakage, double *keff) {
+  int rc = usable(p);
+  if (rc != MOC_OK) return rc;
+  cudaSetDevice(p->device);
+  rc = moc_launch_keff(p, leakage);
+  if (rc != MOC_OK) return fail(p, rc);
+  double sc[SC_COUNT];
+  rc = read_scalars(p, sc);
+  if (rc != MOC_OK) return rc;
+  if (keff) *keff = sc[SC_KEFF];
+  return MOC_OK;
+}
+
+int moc_power_iteration(moc_problem *p, double keff_in, double *keff_out, double *residual) {
+  int rc = usable(p);
+  if (rc != MOC_OK) return rc;
+  if (!(keff_in != 0.0)) return MOC_ERR_ARG;
+  cudaSetDevice(p->device);
+  rc = sweep_impl(p);
+  if (rc != MOC_OK) return rc;
+  rc = moc_launch_renormalize(p);
+  if (rc != MOC_OK) return fail(p, rc);
+  rc = moc_launch_update(p, keff_in, false, true);
+  if (rc != MOC_OK) return fail(p, rc);
+  if (keff_out || residual) {
+    double sc[SC_COUNT];
+    rc = read_scalars(p, sc);
+    if (rc != MOC_OK) return rc;
+    if (keff_out) *keff_out = sc[SC_KEFF];
+    if (residual) *residual = sc[SC_RESIDUAL];
+  }
+  return MOC_OK;
+}
+
+int moc_synchronize(moc_problem *p) {
+  int rc = usable(p);
+  if (rc != MOC_OK) return rc;
+  return sync_check(p);
+}
+
+int moc_time_sweep(moc_problem *p, int iters, double *ms_per_sweep) {
+  int rc = usable(p);
+  if (rc != MOC_OK) return rc;
+  if (iters < 1 || !ms_per_sweep) return MOC_ERR_ARG;
+  cudaSetDevice(p->device);
+  double total = 0.0;
+  for (int i = 0; i < iters; ++i) {
+    if (cudaEventRecord(p->ev0, p->stream) != cudaSuccess) return fail(p, MOC_ERR_CUDA);
+    rc = moc_launch_sweep(p);
+    if (rc != MOC_OK) return fail(p, rc);
+    if (cudaEventRecord(p->ev1, p->stream) != cudaSuccess) return fail(p, MOC_ERR_CUDA);
+    if (cudaEventSynchronize(p->ev1) != cudaSuccess) return fail(p, MOC_ERR_CUDA);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, p->ev0, p->ev1);
+    total += ms;
+  }
+  *ms_per_sweep = total / iters;
+  return sync_check(p);
+}
+
+int moc_time_power_iterations(moc_problem *p, int iters, double *ms_total, double *ms_sweeps,
+                              double *keff, double *residual) {
+  int rc = usable(p);
+  if (rc != MOC_OK) return rc;
+  if (iters < 1) return MOC_ERR_ARG;
+  cudaSetDevice(p->device);
+  std::vector<cudaEvent_t> ev((size_t)(2 * iters + 2), nullptr);
+  for (auto &e : ev)
+    if (cudaEventCreate(&e) != cudaSuccess) {
+      for (auto &x : ev)
+        if (x) cudaEventDestroy(x);
+      return fail(p, MOC_ERR_CUDA);
+    }
+  rc = MOC_OK;
+  cudaEventRecord(ev[0], p->stream);
+  for (int i = 0; i < iters && rc == MOC_OK; ++i) {
+    cudaEventRecord(ev[2 + 2 * i], p->stream);
+    rc = sweep_impl(p);
+    cudaEventRecord(ev[3 + 2 * i], p->stream);
+    if (rc == MOC_OK) rc = moc_launch_renormalize(p);
+    if (rc == MOC_OK) rc = moc_launch_update(p, 0.0, true, true);
+  }
+  cudaEventRecord(ev[1], p->stream);
+  if (rc == MOC_OK && cudaEventSynchronize(ev[1]) != cudaSuccess) rc = MOC_ERR_CUDA;
+  double sweeps = 0.0;
+  float tot = 0.f;
+  if (rc == MOC_OK) {
+    cudaEventElapsedTime(&tot, ev[0], ev[1]);
+    for (int i = 0; i < iters; ++i) {
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, ev[2 + 2 * i], ev[3 + 2 * i]);
+      sweeps += ms;
+    }
+  }
+  for (auto &e : ev) cudaEventDestroy(e);
+  if (rc != MOC_OK) return fail(p, rc);
+  if (ms_total) *ms_total = tot;
+  if (ms_sweeps) *ms_sweeps = sweeps;
+  double sc[SC_COUNT];
+  rc = read_scalars(p, sc);
+  if (rc != MOC_OK) return rc;
+  if (keff) *keff = sc[SC_KEFF];
+  if (residual) *residual = sc[SC_RESIDUAL];
+  return MOC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,106 @@
+// moc_internal.h -- device-side problem state shared by the library's
+// translation units (not part of the public ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "simplemoc_gb300.h"
+
+// Coefficients stored per (sigma_t row, group), as 8 planes of ldg floats:
+//   0 sigT   1 sigT^2   2 sigT*sigT^2   3 (3 sigT^2) sigT^2
+//   4..7 the correctly rounded float reciprocals of planes 0..3.
+// The products are formed in the reference's operand order
+// (src/solver.c:153,176,198) so they equal the reference's divisors bit for bit.
+enum { COEF_PLANES = 8 };
+
+struct SweepArgs {
+  const float *seg_ds;      // [N2D*P*S] 3D segment length per (2D track, polar, seg)
+  const int32_t *seg_src;   // [N3D*S]
+  const float *weight;      // [N3D]  p_weight * az_weight (float, reference order)
+  const float *z0;          // [N3D]
+  const float *mu;          // [P]
+  const int32_t *src_sigt;  // [NS]
+  const float *coef;        // [n_sigt][8][ldg]
+  const float2 *table;      // [N] (slope, intercept)
+  const float *q;           // [NS*F*ldg]
+  float *phi;               // [NS*F*ldg]
+  float *phi_lo;            // [NS*F*ldg] compensation words (MIXED + flag) or null
+  float *psi;               // [N3D*ldg]  forward angular flux, in place
+  const double *q64;        // FP64 mode state
+  double *phi64;
+  double *psi64;
+  int64_t n3d;
+  int64_t ns;               // source regions (bound of seg_src)
+  int32_t G, ldg, nchunk;   // groups, padded stride, ldg/4
+  int32_t F, P, Z, S;
+  int32_t axial_exp;
+  int32_t table_n;
+  float table_dx, table_rdx, table_halfdx, table_maxval;
+  float dz, rdz;            // fine interval height and its reciprocal
+  float d1, rd1, d2, rd2;   // 2 dz and 2 dz dz, and reciprocals
+  float hd;                 // domain height
+  int32_t *err;             // device error word (0 = ok)
+};
+
+struct moc_problem {
+  moc_dims d;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int status = MOC_OK;
+  int mode = MOC_MODE_PLAIN;
+  int flags = 0;
+  int tpw = 0, cpl = 0;          // 0 = automatic
+  int64_t launches = 0;
+  int64_t n3d = 0, nfsr = 0;
+  int32_t ldg = 0;
+  int64_t bytes = 0;
+  // inputs
+  float *seg_ds = nullptr;
+  int32_t *seg_src = nullptr;
+  float *weight = nullptr, *z0 = nullptr, *mu = nullptr;
+  int32_t *src_sigt = nullptr, *src_xs = nullptr;
+  float *vol = nullptr, *coef = nullptr, *xs = nullptr, *scatter_t = nullptr;
+  float *table = nullptr;
+  // state
+  float *q = nullptr, *phi = nullptr, *phi_lo = nullptr, *psi_f = nullptr, *psi_b = nullptr;
+  double *q64 = nullptr, *phi64 = nullptr, *psi_f64 = nullptr, *psi_b64 = nullptr;
+  // reductions / scalars
+  double *partials = nullptr;    // [3 * RED_BLOCKS]
+  double *scalars = nullptr;     // see post kernels
+  int32_t *err = nullptr;
+  int32_t red_blocks = 0;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // host copies needed for re-upload and derived arrays
+  float polar[64];
+};
+
+// Launchers implemented in moc_sweep.cu / moc_post.cu.
+int moc_launch_sweep(moc_problem *p);
+int moc_sweep_launch_shape(const moc_problem *p, int *tpw, int *cpl);
+int moc_launch_renormalize(moc_problem *p);
+int moc_launch_update(moc_problem *p, double keff, bool keff_on_device, bool with_keff);
+int moc_set_leakage(moc_problem *p, double leakage);
+int moc_launch_keff(moc_problem *p, double leakage);
+int moc_post_scratch_blocks();
+
+// Scalars slots in p->scalars (double):
+enum {
+  SC_TOTAL_FISSION = 0,   // renormalize: total fission rate
+  SC_NORM = 1,            // renormalize: norm factor (as applied)
+  SC_RESIDUAL = 2,        // update_sources residual
+  SC_ABS = 3,             // compute_keff absorption
+  SC_FISSION = 4,         // compute_keff fission
+  SC_KEFF = 5,            // compute_keff result
+  SC_KEFF_IN = 6,         // keff used by update_sources
+  SC_LEAKAGE = 7,
+  SC_COUNT = 8
+};
+
+#define MOC_CUDA_TRY(expr)                                                     \
+  do {                                                                         \
+    cudaError_t e_ = (expr);                                                   \
+    if (e_ != cudaSuccess) {                                                   \
+      return (e_ == cudaErrorMemoryAllocation) ? MOC_ERR_OOM : MOC_ERR_CUDA;   \
+    }                                                                          \
+  } while (0)

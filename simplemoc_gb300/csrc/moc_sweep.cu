@@ -1,0 +1,567 @@
+// moc_sweep.cu -- the transport-sweep kernel (replaces transport_sweep and
+// attenuate_fluxes / attenuate_FSR_fluxes, src/solver.c:14-552).
+//
+// Mapping: a group of TPW threads owns one 3D track; thread `li` of the group
+// owns the 4-group chunks li, li+TPW, ... (CPL of them) and keeps their angular
+// flux in registers for the whole track.  The segment streams (3D length and
+// source region) are read TPW entries at a time, one per thread, and broadcast
+// with warp shuffles.  Per segment every thread gathers its chunks of the three
+// neighbouring fine-source rows (one 16-byte load per row, not allocated in
+// L1), forms the quadratic source, attenuates, and adds its tally chunk with a
+// single vector reduction (red.global.add.v4.f32).  The grid is persistent:
+// one wave of resident blocks walks all tracks.
+//
+// Modes:
+//  PLAIN  every float operation of src/solver.c:38-279 in the reference order,
+//         with no contraction; divisions by per-material or per-problem
+//         constants use a correctly rounded quotient built from the precomputed
+//         reciprocal (one FMA correction, Markstein), and the exponential comes
+//         from the reference table (src/solver.c:1441-1464).  psi is
+//         bit-identical to the reference's.
+//  MIXED  contracted FP32 with reciprocals and an accurate 1-exp(-tau).
+//  FP64   double state and arithmetic, exact 1-exp(-tau) (expm1).
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "moc_internal.h"
+
+namespace {
+
+constexpr int MODE_PLAIN = MOC_MODE_PLAIN;
+constexpr int MODE_MIXED = MOC_MODE_MIXED;
+constexpr int MODE_FP64 = MOC_MODE_FP64;
+constexpr int BLOCK = 256;
+constexpr unsigned FULL = 0xffffffffu;
+
+// a / b correctly rounded, given rb = RN(1/b): q = a*rb, r = a - b*q (exact),
+// q + r*rb (P. Markstein, IBM J. Res. Dev. 34(1), 1990).
+__device__ __forceinline__ float div_cr(float a, float b, float rb) {
+  float q = __fmul_rn(a, rb);
+  float r = __fmaf_rn(-q, b, a);
+  return __fmaf_rn(r, rb, q);
+}
+
+__device__ __forceinline__ float4 ld_stream(const float *p) {
+  float4 v;
+  asm volatile("ld.global.nc.L1::no_allocate.v4.f32 {%0,%1,%2,%3}, [%4];"
+               : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+               : "l"(p));
+  return v;
+}
+
+__device__ __forceinline__ void red_add_v4(float *p, float a, float b, float c, float d) {
+  asm volatile("red.global.add.v4.f32 [%0], {%1,%2,%3,%4};" ::"l"(p), "f"(a), "f"(b),
+               "f"(c), "f"(d)
+               : "memory");
+}
+
+__device__ __forceinline__ float get(const float4 &v, int e) {
+  return e == 0 ? v.x : e == 1 ? v.y : e == 2 ? v.z : v.w;
+}
+__device__ __forceinline__ void set(float4 &v, int e, float x) {
+  if (e == 0) v.x = x;
+  else if (e == 1) v.y = x;
+  else if (e == 2) v.z = x;
+  else v.w = x;
+}
+
+// Reference interpolation table, src/solver.c:1441-1464.
+__device__ __forceinline__ float table_lookup(const SweepArgs &a, const float2 *tab, float x) {
+  if (x > a.table_maxval) return 1.0f;
+  int idx = __float2int_rz(__fadd_rn(div_cr(x, a.table_dx, a.table_rdx), a.table_halfdx));
+  idx = max(0, min(idx, a.table_n - 1));
+  float2 se = tab[idx];
+  return __fadd_rn(__fmul_rn(se.x, x), se.y);
+}
+
+// 1 - exp(-tau) to ~1e-7 relative: Taylor series below 0.5, SFU exponential above.
+__device__ __forceinline__ float one_minus_exp(float t) {
+  float s = fmaf(t, -1.0f / 362880.0f, 1.0f / 40320.0f);
+  s = fmaf(t, s, -1.0f / 5040.0f);
+  s = fmaf(t, s, 1.0f / 720.0f);
+  s = fmaf(t, s, -1.0f / 120.0f);
+  s = fmaf(t, s, 1.0f / 24.0f);
+  s = fmaf(t, s, -1.0f / 6.0f);
+  s = fmaf(t, s, 0.5f);
+  s = fmaf(t, -s, 1.0f);
+  float small = t * s;
+  float big = 1.0f - __expf(-t);
+  return t < 0.5f ? small : big;
+}
+
+struct Seg {
+  float zin;      // height within the fitted interval (after edge shift)
+  int64_t qrow;   // first of the three fine-source rows (quadratic) or the row (flat)
+  int64_t frow;   // tally row
+  int64_t crow;   // coefficient block
+};
+
+__device__ __forceinline__ Seg segment_geometry(const SweepArgs &a, float z, int s) {
+  Seg g;
+  // src/solver.c:38-45 (z / dz once: both uses are the same expression)
+  int zi = __float2int_rz(div_cr(z, a.dz, a.rdz));
+  float zin = __fsub_rn(z, __fmul_rn(a.dz, __fadd_rn(__int2float_rn(zi), 0.5f)));
+  int fine = zi % a.F;
+  int r0 = fine;
+  if (a.axial_exp == 2) {
+    if (fine == 0) {                     // src/solver.c:55-58
+      zin = __fsub_rn(zin, a.dz);
+      r0 = 0;
+    } else if (fine == a.F - 1) {        // src/solver.c:84-87
+      zin = __fadd_rn(zin, a.dz);
+      r0 = fine - 2;
+    } else {
+      r0 = fine - 1;
+    }
+  }
+  g.zin = zin;
+  int64_t base = (int64_t)s * a.F;
+  g.qrow = (base + r0) * a.ldg;
+  g.frow = (base + fine) * a.ldg;
+  g.crow = (int64_t)__ldg(a.src_sigt + s) * COEF_PLANES * a.ldg;
+  return g;
+}
+
+__device__ __forceinline__ float advance_z(const SweepArgs &a, float z, float ds, float mu) {
+  z = __fadd_rn(z, __fmul_rn(ds, mu));
+  // |ds*mu| < domain height is checked at upload, so one pass of each suffices;
+  // the bound keeps the loop finite whatever the input.
+#pragma unroll 1
+  for (int it = 0; it < 4 && z >= a.hd; ++it) z = __fsub_rn(z, a.hd);
+#pragma unroll 1
+  for (int it = 0; it < 4 && z < 0.0f; ++it) z = __fadd_rn(z, a.hd);
+  return z;
+}
+
+// ---- PLAIN arithmetic for one group, quadratic source (src/solver.c:74-278)
+__device__ __forceinline__ float plain_quad(const SweepArgs &a, const float2 *tab, float y1,
+                                            float y2, float y3, float sig, float sig2,
+                                            float sig3, float sig4, float r1, float r2,
+                                            float r3, float r4, float zin, float ds,
+                                            float mu, float mu2, float w, float &p) {
+  float c0 = y2;
+  float c1 = div_cr(__fsub_rn(y1, y3), a.d1, a.rd1);
+  float c2 = div_cr(__fadd_rn(__fsub_rn(y1, __fmul_rn(2.f, y2)), y3), a.d2, a.rd2);
+  float q0 = __fadd_rn(__fadd_rn(c0, __fmul_rn(c1, zin)), __fmul_rn(__fmul_rn(c2, zin), zin));
+  float q1 = __fadd_rn(c1, __fmul_rn(__fmul_rn(2.f, c2), zin));
+  float q2 = c2;
+  float tau = __fmul_rn(sig, ds);
+  float e = table_lookup(a, tab, tau);
+  float reuse = __fadd_rn(__fmul_rn(tau, __fsub_rn(tau, 2.f)), div_cr(__fmul_rn(2.f, e), sig3, r3));
+  float A = div_cr(__fadd_rn(__fmul_rn(q0, tau), __fmul_rn(__fsub_rn(__fmul_rn(sig, p), q0), e)),
+                   sig2, r2);
+  float B = __fmul_rn(__fmul_rn(q1, mu), reuse);
+  float cub = __fsub_rn(__fmul_rn(tau, __fadd_rn(__fmul_rn(tau, __fsub_rn(tau, 3.f)), 6.f)),
+                        __fmul_rn(6.f, e));
+  float C = div_cr(__fmul_rn(__fmul_rn(q2, mu2), cub), sig4, r4);
+  float fi = __fadd_rn(__fadd_rn(A, B), C);
+  float t1 = div_cr(__fmul_rn(q0, e), sig, r1);
+  float t2 = div_cr(__fmul_rn(__fmul_rn(q1, mu), __fsub_rn(tau, e)), sig2, r2);
+  float t3 = __fmul_rn(__fmul_rn(q2, mu2), reuse);
+  float t4 = __fmul_rn(p, __fsub_rn(1.f, e));
+  p = __fadd_rn(__fadd_rn(__fadd_rn(t1, t2), t3), t4);
+  return __fmul_rn(w, fi);
+}
+
+// ---- PLAIN flat source (src/solver.c:1075-1115)
+__device__ __forceinline__ float plain_flat(const SweepArgs &a, const float2 *tab, float y,
+                                            float sig, float r1, float ds, float w_mu,
+                                            float &p) {
+  float tau = __fmul_rn(sig, ds);
+  float e = table_lookup(a, tab, tau);
+  float qq = div_cr(y, sig, r1);
+  float dpsi = __fmul_rn(__fsub_rn(p, qq), e);
+  p = __fsub_rn(p, dpsi);
+  return __fmul_rn(w_mu, dpsi);
+}
+
+// ---- MIXED arithmetic, quadratic source
+__device__ __forceinline__ float mixed_quad(const SweepArgs &a, float y1, float y2, float y3,
+                                            float sig, float r1, float r2, float r3, float r4,
+                                            float zin, float ds, float mu, float mu2, float w,
+                                            float &p) {
+  float c1 = (y1 - y3) * a.rd1;
+  float c2 = (fmaf(-2.f, y2, y1) + y3) * a.rd2;
+  float q0 = fmaf(fmaf(c2, zin, c1), zin, y2);
+  float q1 = fmaf(2.f * c2, zin, c1);
+  float tau = sig * ds;
+  float e = one_minus_exp(tau);
+  float reuse = fmaf(tau, tau - 2.f, 2.f * e * r3);
+  float A = fmaf(q0, tau, fmaf(sig, p, -q0) * e) * r2;
+  float q1mu = q1 * mu;
+  float q2mu2 = c2 * mu2;
+  float cub = fmaf(tau, fmaf(tau, tau - 3.f, 6.f), -6.f * e);
+  float fi = fmaf(q2mu2 * cub, r4, fmaf(q1mu, reuse, A));
+  float pn = fmaf(q0 * e, r1, fmaf(q1mu * (tau - e), r2, fmaf(q2mu2, reuse, p * (1.f - e))));
+  p = pn;
+  return w * fi;
+}
+
+__device__ __forceinline__ float mixed_flat(float y, float sig, float r1, float ds, float w_mu,
+                                            float &p) {
+  float e = one_minus_exp(sig * ds);
+  float dpsi = (p - y * r1) * e;
+  p -= dpsi;
+  return w_mu * dpsi;
+}
+
+// Compensated tally: hi word by atomic add returning the old value, the
+// rounding error of that add (TwoSum) into the lo word.
+__device__ __forceinline__ void comp_add(float *hi, float *lo, float x) {
+  float old = atomicAdd(hi, x);
+  float s = old + x;
+  float bp = s - old;
+  float err = (old - (s - bp)) + (x - bp);
+  if (err != 0.0f) atomicAdd(lo, err);
+}
+
+template <int TPW, int CPL, int MODE, bool QUAD>
+__global__ void __launch_bounds__(BLOCK) sweep_kernel(SweepArgs a) {
+  extern __shared__ float2 s_table[];
+  if (MODE == MODE_PLAIN) {
+    for (int i = threadIdx.x; i < a.table_n; i += BLOCK) s_table[i] = a.table[i];
+    __syncthreads();
+  }
+  constexpr int GPW = 32 / TPW;
+  const int lane = threadIdx.x & 31;
+  const int li = lane % TPW;
+  const int gw = lane / TPW;
+  const int64_t warp_id = ((int64_t)blockIdx.x * BLOCK + threadIdx.x) >> 5;
+  const int64_t n_warps = ((int64_t)gridDim.x * BLOCK) >> 5;
+  const int64_t PZ = (int64_t)a.P * a.Z;
+
+  for (int64_t base = warp_id * GPW; base < a.n3d; base += n_warps * GPW) {
+    const int64_t track = base + gw;
+    const bool valid = track < a.n3d;
+    const int64_t tr = valid ? track : a.n3d - 1;
+    const int64_t i2 = tr / PZ;
+    const int j = (int)((tr / a.Z) % a.P);
+    const float mu = a.mu[j];
+    const float mu2 = __fmul_rn(mu, mu);
+    const float w = a.weight[tr];
+    const float w_mu = __fmul_rn(w, mu);
+    float z = a.z0[tr];
+    const float *dsb = a.seg_ds + (i2 * a.P + j) * a.S;
+    const int32_t *srcb = a.seg_src + tr * a.S;
+
+    float4 psi[CPL];
+#pragma unroll
+    for (int k = 0; k < CPL; ++k) {
+      const int c = li + TPW * k;
+      psi[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (c < a.nchunk) psi[k] = *reinterpret_cast<const float4 *>(a.psi + tr * a.ldg + 4 * c);
+    }
+
+    for (int n0 = 0; n0 < a.S; n0 += TPW) {
+      const int nl = n0 + li;
+      const float my_ds = nl < a.S ? __ldg(dsb + nl) : 0.f;
+      const int my_src = nl < a.S ? __ldg(srcb + nl) : 0;
+      const int cnt = min(TPW, a.S - n0);
+      for (int nn = 0; nn < cnt; ++nn) {
+        const float ds = __shfl_sync(FULL, my_ds, nn, TPW);
+        int s = __shfl_sync(FULL, my_src, nn, TPW);
+        if ((uint32_t)s >= (uint64_t)a.ns) {   // checked at upload; never trusted blindly
+          if (li == 0) atomicOr(a.err, 1);
+          s = 0;
+        }
+        const Seg g = segment_geometry(a, z, s);
+#pragma unroll
+        for (int k = 0; k < CPL; ++k) {
+          const int c = li + TPW * k;
+          if (c >= a.nchunk) continue;
+          const int g4 = 4 * c;
+          const float *cf = a.coef + g.crow + g4;
+          const float4 sig = __ldg(reinterpret_cast<const float4 *>(cf));
+          const float4 r1 = __ldg(reinterpret_cast<const float4 *>(cf + 4 * a.ldg));
+          float4 t;
+          if (QUAD) {
+            const float *qr = a.q + g.qrow + g4;
+            const float4 y1 = ld_stream(qr);
+            const float4 y2 = ld_stream(qr + a.ldg);
+            const float4 y3 = ld_stream(qr + 2 * a.ldg);
+            const float4 r2 = __ldg(reinterpret_cast<const float4 *>(cf + 5 * a.ldg));
+            const float4 r3 = __ldg(reinterpret_cast<const float4 *>(cf + 6 * a.ldg));
+            const float4 r4 = __ldg(reinterpret_cast<const float4 *>(cf + 7 * a.ldg));
+            if (MODE == MODE_PLAIN) {
+              const float4 sig2 = __ldg(reinterpret_cast<const float4 *>(cf + 1 * a.ldg));
+              const float4 sig3 = __ldg(reinterpret_cast<const float4 *>(cf + 2 * a.ldg));
+              const float4 sig4 = __ldg(reinterpret_cast<const float4 *>(cf + 3 * a.ldg));
+#pragma unroll
+              for (int e = 0; e < 4; ++e) {
+                float p = get(psi[k], e);
+                set(t, e, plain_quad(a, s_table, get(y1, e), get(y2, e), get(y3, e), get(sig, e),
+                                     get(sig2, e), get(sig3, e), get(sig4, e), get(r1, e),
+                                     get(r2, e), get(r3, e), get(r4, e), g.zin, ds, mu, mu2, w,
+                                     p));
+                set(psi[k], e, p);
+              }
+            } else {
+#pragma unroll
+              for (int e = 0; e < 4; ++e) {
+                float p = get(psi[k], e);
+                set(t, e, mixed_quad(a, get(y1, e), get(y2, e), get(y3, e), get(sig, e),
+                                     get(r1, e), get(r2, e), get(r3, e), get(r4, e), g.zin, ds,
+                                     mu, mu2, w, p));
+                set(psi[k], e, p);
+              }
+            }
+          } else {
+            const float4 y = ld_stream(a.q + g.qrow + g4);
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+              float p = get(psi[k], e);
+              if (MODE == MODE_PLAIN)
+                set(t, e, plain_flat(a, s_table, get(y, e), get(sig, e), get(r1, e), ds, w_mu, p));
+              else
+                set(t, e, mixed_flat(get(y, e), get(sig, e), get(r1, e), ds, w_mu, p));
+              set(psi[k], e, p);
+            }
+          }
+          if (valid) {
+            float *dst = a.phi + g.frow + g4;
+            if (MODE == MODE_MIXED && a.phi_lo != nullptr) {
+              float *lo = a.phi_lo + g.frow + g4;
+              comp_add(dst + 0, lo + 0, t.x);
+              comp_add(dst + 1, lo + 1, t.y);
+              comp_add(dst + 2, lo + 2, t.z);
+              comp_add(dst + 3, lo + 3, t.w);
+            } else {
+              red_add_v4(dst, t.x, t.y, t.z, t.w);
+            }
+          }
+        }
+        z = advance_z(a, z, ds, mu);
+      }
+    }
+    if (valid) {
+#pragma unroll
+      for (int k = 0; k < CPL; ++k) {
+        const int c = li + TPW * k;
+        if (c < a.nchunk) *reinterpret_cast<float4 *>(a.psi + tr * a.ldg + 4 * c) = psi[k];
+      }
+    }
+  }
+}
+
+// ---- FP64 yardstick: same traversal, double state, exact 1-exp(-tau).
+template <int TPW, bool QUAD>
+__global__ void __launch_bounds__(BLOCK) sweep64_kernel(SweepArgs a) {
+  const int lane = threadIdx.x & 31;
+  const int li = lane % TPW;
+  const int gw = lane / TPW;
+  constexpr int GPW = 32 / TPW;
+  const int64_t warp_id = ((int64_t)blockIdx.x * BLOCK + threadIdx.x) >> 5;
+  const int64_t n_warps = ((int64_t)gridDim.x * BLOCK) >> 5;
+  const int64_t PZ = (int64_t)a.P * a.Z;
+  for (int64_t base = warp_id * GPW; base < a.n3d; base += n_warps * GPW) {
+    const int64_t track = base + gw;
+    const bool valid = track < a.n3d;
+    const int64_t tr = valid ? track : a.n3d - 1;
+    const int64_t i2 = tr / PZ;
+    const int j = (int)((tr / a.Z) % a.P);
+    const float muf = a.mu[j];
+    const double mu = muf, mu2 = mu * mu;
+    const double w = a.weight[tr];     // reference weight, promoted
+    float z = a.z0[tr];
+    const float *dsb = a.seg_ds + (i2 * a.P + j) * a.S;
+    const int32_t *srcb = a.seg_src + tr * a.S;
+    for (int n = 0; n < a.S; ++n) {
+      const float dsf = __ldg(dsb + n);
+      int s = __ldg(srcb + n);
+      if ((uint32_t)s >= (uint64_t)a.ns) {
+        if (li == 0) atomicOr(a.err, 1);
+        s = 0;
+      }
+      const double ds = dsf;
+      const int zi = __float2int_rz(div_cr(z, a.dz, a.rdz));
+      const int fine = zi % a.F;
+      const double dz = a.dz;
+      double zin = (double)z - dz * (zi + 0.5);
+      int r0 = fine;
+      if (QUAD) {
+        if (fine == 0) { zin -= dz; r0 = 0; }
+        else if (fine == a.F - 1) { zin += dz; r0 = fine - 2; }
+        else r0 = fine - 1;
+      }
+      const int64_t sb = (int64_t)s * a.F;
+      const double *qr = a.q64 + (sb + r0) * a.ldg;
+      double *fr = a.phi64 + (sb + fine) * a.ldg;
+      const float *sigr = a.coef + (int64_t)__ldg(a.src_sigt + s) * COEF_PLANES * a.ldg;
+      for (int g = li; g < a.G; g += TPW) {
+        const double sig = sigr[g];
+        const double tau = sig * ds;
+        const double e = -expm1(-tau);
+        double p = a.psi64[tr * a.ldg + g];
+        double tally;
+        if (QUAD) {
+          const double y1 = qr[g], y2 = qr[a.ldg + g], y3 = qr[2 * a.ldg + g];
+          const double c1 = (y1 - y3) / (2.0 * dz);
+          const double c2 = (y1 - 2.0 * y2 + y3) / (2.0 * dz * dz);
+          const double q0 = y2 + c1 * zin + c2 * zin * zin;
+          const double q1 = c1 + 2.0 * c2 * zin;
+          const double sig2 = sig * sig;
+          const double reuse = tau * (tau - 2.0) + 2.0 * e / (sig * sig2);
+          const double fi = (q0 * tau + (sig * p - q0) * e) / sig2 + q1 * mu * reuse +
+                            c2 * mu2 * (tau * (tau * (tau - 3.0) + 6.0) - 6.0 * e) /
+                                (3.0 * sig2 * sig2);
+          tally = w * fi;
+          p = q0 * e / sig + q1 * mu * (tau - e) / sig2 + c2 * mu2 * reuse + p * (1.0 - e);
+        } else {
+          const double dpsi = (p - qr[g] / sig) * e;
+          p -= dpsi;
+          tally = w * mu * dpsi;
+        }
+        if (valid) {
+          a.psi64[tr * a.ldg + g] = p;
+          atomicAdd(fr + g, tally);
+        }
+      }
+      z = advance_z(a, z, dsf, muf);
+    }
+  }
+}
+
+template <int TPW, int CPL, int MODE, bool QUAD>
+int launch_t(moc_problem *p, const SweepArgs &a) {
+  auto kern = sweep_kernel<TPW, CPL, MODE, QUAD>;
+  size_t smem = (MODE == MODE_PLAIN) ? sizeof(float2) * (size_t)a.table_n : 0;
+  if (smem > 48 * 1024) {
+    if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+        cudaSuccess)
+      return MOC_ERR_UNSUPPORTED;
+  }
+  int per_sm = 0, sms = 0;
+  MOC_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BLOCK, smem));
+  MOC_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p->device));
+  if (per_sm < 1) return MOC_ERR_UNSUPPORTED;
+  int64_t groups = (a.n3d + (32 / TPW) - 1) / (32 / TPW);         // warps of work
+  int64_t blocks_needed = (groups + (BLOCK / 32) - 1) / (BLOCK / 32);
+  int64_t grid = (int64_t)per_sm * sms;
+  if (grid > blocks_needed) grid = blocks_needed;
+  if (grid < 1) grid = 1;
+  kern<<<(unsigned)grid, BLOCK, smem, p->stream>>>(a);
+  MOC_CUDA_TRY(cudaGetLastError());
+  p->launches++;
+  return MOC_OK;
+}
+
+template <int TPW, bool QUAD>
+int launch64_t(moc_problem *p, const SweepArgs &a) {
+  auto kern = sweep64_kernel<TPW, QUAD>;
+  int per_sm = 0, sms = 0;
+  MOC_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BLOCK, 0));
+  MOC_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p->device));
+  int64_t warps = (a.n3d + (32 / TPW) - 1) / (32 / TPW);
+  int64_t grid = (int64_t)per_sm * sms;
+  int64_t need = (warps + 7) / 8;
+  if (grid > need) grid = need;
+  if (grid < 1) grid = 1;
+  kern<<<(unsigned)grid, BLOCK, 0, p->stream>>>(a);
+  MOC_CUDA_TRY(cudaGetLastError());
+  p->launches++;
+  return MOC_OK;
+}
+
+template <int MODE, bool QUAD>
+int dispatch_shape(moc_problem *p, const SweepArgs &a, int tpw, int cpl) {
+  if (tpw == 32 && cpl == 1) return launch_t<32, 1, MODE, QUAD>(p, a);
+  if (tpw == 32 && cpl == 2) return launch_t<32, 2, MODE, QUAD>(p, a);
+  if (tpw == 32 && cpl == 4) return launch_t<32, 4, MODE, QUAD>(p, a);
+  if (tpw == 16 && cpl == 1) return launch_t<16, 1, MODE, QUAD>(p, a);
+  if (tpw == 16 && cpl == 2) return launch_t<16, 2, MODE, QUAD>(p, a);
+  if (tpw == 8 && cpl == 1) return launch_t<8, 1, MODE, QUAD>(p, a);
+  if (tpw == 8 && cpl == 4) return launch_t<8, 4, MODE, QUAD>(p, a);
+  if (tpw == 4 && cpl == 2) return launch_t<4, 2, MODE, QUAD>(p, a);
+  return MOC_ERR_UNSUPPORTED;
+}
+
+}  // namespace
+
+// Chooses the threads-per-track and chunks-per-thread for a group count: the
+// smallest shape whose TPW*CPL chunks cover the ldg/4 chunks, preferring more
+// threads per track (more tracks in flight per SM is what hides gather latency).
+int moc_sweep_launch_shape(const moc_problem *p, int *tpw, int *cpl) {
+  int nchunk = p->ldg / 4;
+  if (p->tpw > 0) {
+    *tpw = p->tpw;
+    *cpl = p->cpl;
+    if ((int64_t)p->tpw * p->cpl < nchunk) return MOC_ERR_ARG;
+    return MOC_OK;
+  }
+  static const int shapes[][2] = {{4, 2}, {8, 1}, {16, 1}, {8, 4}, {32, 1}, {16, 2},
+                                  {32, 2}, {32, 4}};
+  // prefer the shape with the best lane utilisation, then the fewest chunks per thread
+  int best = -1;
+  double best_util = -1.0;
+  for (int i = 0; i < 8; ++i) {
+    int cap = shapes[i][0] * shapes[i][1];
+    if (cap < nchunk) continue;
+    double util = (double)nchunk / cap;
+    if (util > best_util + 1e-9 ||
+        (util > best_util - 1e-9 && best >= 0 && shapes[i][1] < shapes[best][1])) {
+      best = i;
+      best_util = util;
+    }
+  }
+  if (best < 0) return MOC_ERR_UNSUPPORTED;
+  *tpw = shapes[best][0];
+  *cpl = shapes[best][1];
+  return MOC_OK;
+}
+
+int moc_launch_sweep(moc_problem *p) {
+  const moc_dims &d = p->d;
+  SweepArgs a{};
+  a.seg_ds = p->seg_ds;
+  a.seg_src = p->seg_src;
+  a.weight = p->weight;
+  a.z0 = p->z0;
+  a.mu = p->mu;
+  a.src_sigt = p->src_sigt;
+  a.coef = p->coef;
+  a.table = reinterpret_cast<const float2 *>(p->table);
+  a.q = p->q;
+  a.phi = p->phi;
+  a.phi_lo = (p->mode == MOC_MODE_MIXED && (p->flags & MOC_FLAG_COMPENSATED)) ? p->phi_lo : nullptr;
+  a.psi = p->psi_f;
+  a.q64 = p->q64;
+  a.phi64 = p->phi64;
+  a.psi64 = p->psi_f64;
+  a.n3d = p->n3d;
+  a.ns = d.n_sources;
+  a.G = d.n_groups;
+  a.ldg = p->ldg;
+  a.nchunk = p->ldg / 4;
+  a.F = d.fai;
+  a.P = d.n_polar;
+  a.Z = d.z_stacked;
+  a.S = d.n_seg;
+  a.axial_exp = d.axial_exp;
+  a.table_n = d.table_n;
+  a.table_dx = d.table_dx;
+  a.table_rdx = 1.0f / d.table_dx;
+  a.table_halfdx = 0.5f * d.table_dx;
+  a.table_maxval = d.table_maxval;
+  // src/solver.c:38 -- float height over the int product
+  a.dz = d.height / (float)(d.fai * d.decomp_ax * d.cai);
+  a.rdz = 1.0f / a.dz;
+  a.d1 = 2.f * a.dz;                      // src/solver.c:75
+  a.rd1 = 1.0f / a.d1;
+  a.d2 = 2.f * a.dz * a.dz;               // src/solver.c:76
+  a.rd2 = 1.0f / a.d2;
+  a.hd = d.height / (float)d.decomp_ax;
+  a.err = p->err;
+  const bool quad = d.axial_exp == 2;
+  if (p->mode == MOC_MODE_FP64) {
+    if (!p->q64) return MOC_ERR_STATE;
+    return quad ? launch64_t<32, true>(p, a) : launch64_t<32, false>(p, a);
+  }
+  int tpw = 0, cpl = 0;
+  int st = moc_sweep_launch_shape(p, &tpw, &cpl);
+  if (st != MOC_OK) return st;
+  if (p->mode == MOC_MODE_PLAIN)
+    return quad ? dispatch_shape<MODE_PLAIN, true>(p, a, tpw, cpl)
+                : dispatch_shape<MODE_PLAIN, false>(p, a, tpw, cpl);
+  return quad ? dispatch_shape<MODE_MIXED, true>(p, a, tpw, cpl)
+              : dispatch_shape<MODE_MIXED, false>(p, a, tpw, cpl);
+}

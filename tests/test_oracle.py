@@ -1,0 +1,134 @@
+"""CPU tests of the oracle: the C restatement against the reference's golden
+fixtures and, where the reference objects are built, against the reference
+itself on fresh seeded problems."""
+import numpy as np
+import pytest
+
+import oracle
+from tests._util import GOLDEN_CASES, load_golden
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+def test_port_matches_golden_sweep(port, name):
+    hp, z = load_golden(name)
+    st = oracle.fresh_state(hp)
+    op = oracle.make_problem(hp)
+    n = port.sweep(op, st["fine_source"], st["fine_flux"], st["psi_f"])
+    assert n == hp.spec.n_tracks_3d * hp.spec.n_seg
+    # bit-identical to the reference's own attenuate_fluxes
+    assert np.array_equal(st["psi_f"], z["sweep1_psi_f"])
+    assert np.array_equal(st["fine_flux"], z["sweep1_fine_flux"])
+
+
+@pytest.mark.parametrize("name", GOLDEN_CASES)
+def test_port_matches_golden_power_iterations(port, name):
+    hp, z = load_golden(name)
+    st = oracle.fresh_state(hp)
+    hist = port.iterate(hp, st, int(z["iters"]))
+    np.testing.assert_array_equal(np.asarray(hist), z["hist"])
+    for k in ("fine_flux", "fine_source", "psi_f", "psi_b"):
+        assert np.array_equal(st[k], z[f"final_{k}"]), k
+
+
+def test_golden_inputs_reproduced_by_generator(lib):
+    """The seeded generator rebuilds the fixture inputs bit for bit."""
+    import simplemoc_gb300 as sm
+    for name in GOLDEN_CASES:
+        hp, z = load_golden(name)
+        g = sm.generate(hp.spec)
+        for k in ("seg_len", "seg_src", "az_weight", "p_weight", "z0", "polar_angles",
+                  "src_sigt", "src_xs", "vol", "sigt", "xs", "scatter", "fine_source", "table"):
+            assert np.array_equal(getattr(g, k), z[k]), (name, k)
+
+
+@pytest.mark.parametrize("precision", [0.01, 1e-3, 1e-4, 1e-5])
+def test_exp_table_matches_reference(port, ref, lib, precision):
+    import simplemoc_gb300 as sm
+    v_ref, dx_ref, mv_ref, n_ref = ref.exp_table(precision)
+    v_port, dx_port, mv_port, n_port = port.exp_table(precision)
+    v_lib, dx_lib, mv_lib, n_lib = sm.exp_table(precision)
+    assert n_ref == n_port == n_lib
+    assert np.array_equal(v_ref, v_port) and np.array_equal(v_ref, v_lib)
+    assert dx_ref == dx_port == dx_lib and mv_ref == mv_port == mv_lib
+
+
+def test_exp_table_known_values(port):
+    """Values the reference formula gives for precision 0.01 (src/utils.c:54-74)."""
+    v, dx, mv, n = port.exp_table(0.01)
+    assert n == 353                       # (int)(10 * sqrt(1 / 8e-4))
+    assert dx == np.float32(10.0) / np.float32(353)
+    assert v[0] == -1.0 and v[1] == 0.0   # slope -e^0, intercept 1 + (0 - 1) * 1
+    # the reference stores slope -e^{-x0} (the tangent of 1 - e^{-x} has slope
+    # +e^{-x0}); check one interior node against the reference formula
+    k = 100
+    e = np.float32(np.exp(np.float64(np.float32(-k) * np.float32(dx))))
+    assert v[2 * k] == -e
+    assert v[2 * k + 1] == np.float32(1) + (np.float32(k) * np.float32(dx) - np.float32(1)) * e
+
+
+def test_pairwise_sum_order(port):
+    import ctypes as C
+    rng = np.random.default_rng(0)
+    x = rng.random(1000, dtype=np.float32)
+
+    def pw(v):
+        if len(v) <= 16:
+            s = np.float32(0)
+            for t in v:
+                s = np.float32(s + t)
+            return s
+        h = len(v) // 2
+        return np.float32(pw(v[:h]) + pw(v[h:]))
+
+    got = port.lib.oracle_pairwise_sum(x.ctypes.data_as(C.POINTER(C.c_float)), len(x))
+    assert np.float32(got) == pw(x)
+
+
+@pytest.mark.parametrize("axial_exp,groups,fai,seed", [(2, 16, 5, 1), (2, 5, 3, 2), (0, 9, 4, 3),
+                                                       (2, 32, 7, 4)])
+def test_port_matches_reference_fresh_problems(port, ref, lib, axial_exp, groups, fai, seed):
+    import simplemoc_gb300 as sm
+    spec = sm.ProblemSpec(n_groups=groups, fai=fai, cai=3, height=150.0, n_sources=33,
+                          n_tracks_2d=7, n_polar=4, z_stacked=3, n_seg=29,
+                          axial_exp=axial_exp, seed=1000 + seed)
+    hp = sm.generate(spec)
+    a, b = oracle.fresh_state(hp), oracle.fresh_state(hp)
+    ha = port.iterate(hp, a, 3)
+    hb = ref.iterate(hp, b, 3)
+    # the residual is NaN when a region was never visited (old source 0)
+    np.testing.assert_array_equal(np.asarray(ha), np.asarray(hb))
+    for k in a:
+        assert np.array_equal(a[k], b[k]), k
+
+
+def test_openmp_sweep_matches_serial_within_rounding(port, lib):
+    """The locked OpenMP sweep (CPU timing path) computes the same tallies;
+    only the order of additions differs."""
+    import simplemoc_gb300 as sm
+    spec = sm.ProblemSpec(n_groups=20, fai=5, cai=4, n_sources=60, n_tracks_2d=16, n_polar=4,
+                          z_stacked=8, n_seg=50, seed=5)
+    hp = sm.generate(spec)
+    op = oracle.make_problem(hp)
+    a, b = oracle.fresh_state(hp), oracle.fresh_state(hp)
+    port.sweep(op, a["fine_source"], a["fine_flux"], a["psi_f"])
+    port.sweep_omp(op, b["fine_source"], b["fine_flux"], b["psi_f"], 4)
+    assert np.array_equal(a["psi_f"], b["psi_f"])
+    np.testing.assert_allclose(b["fine_flux"], a["fine_flux"], rtol=2e-5, atol=1e-6)
+
+
+def test_fp64_oracle_close_to_fp32_with_fine_table(port, lib):
+    """With a very fine table the FP32 reference formula approaches the FP64
+    yardstick (which uses exact 1-exp(-tau))."""
+    import simplemoc_gb300 as sm
+    spec = sm.ProblemSpec(n_groups=8, fai=5, cai=4, n_sources=40, n_tracks_2d=6, n_polar=4,
+                          z_stacked=4, n_seg=50, precision=1e-7, seed=9)
+    hp = sm.generate(spec)
+    op = oracle.make_problem(hp)
+    a = oracle.fresh_state(hp)
+    d = oracle.fresh_state(hp, np.float64)
+    port.sweep(op, a["fine_source"], a["fine_flux"], a["psi_f"])
+    port.sweep64(op, d["fine_source"], d["fine_flux"], d["psi_f"])
+    # the reference table has the slope-sign defect, so agreement is only to
+    # its error (~2 dx), not to FP32 rounding
+    err = np.abs(a["fine_flux"] - d["fine_flux"]).max() / np.abs(d["fine_flux"]).max()
+    assert err < 5e-3
