@@ -19,6 +19,13 @@ constexpr int RBLOCKS = 1024;      // partials per reduction (fixed: determinist
 constexpr int RTHREADS = 256;
 constexpr double PI = 3.14159265358979323846;
 
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float div_rn(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ double div_rn(double a, double b) { return __ddiv_rn(a, b); }
+
 __device__ __forceinline__ double block_sum(double v, double *sh) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
@@ -135,19 +142,22 @@ __global__ void __launch_bounds__(RTHREADS) update_kernel(
     // fission source of the region (src/solver.c:1266-1271)
     T fis = 0;
     double ab64 = 0.0, fi64 = 0.0;
+    // explicit roundings: the fused (WITH_KEFF) and plain instances must
+    // produce identical sources whatever the compiler's contraction choices
     for (int g = lane; g < G; g += 32) {
       const T v = ph[g];
       myphi[g] = v;
-      fis += v * (T)x[g * 3 + 0];
+      const T fprod = mul_rn(v, (T)x[g * 3 + 0]);
+      fis = add_rn(fis, fprod);
       if (WITH_KEFF) {
-        ab64 += (double)((T)x[g * 3 + 1] * v);
-        fi64 += (double)((T)x[g * 3 + 0] * v);
+        ab64 += (double)mul_rn((T)x[g * 3 + 1], v);
+        fi64 += (double)fprod;
       }
     }
     for (int o = 16; o > 0; o >>= 1) fis += __shfl_xor_sync(0xffffffffu, fis, o);
     __syncwarp();
     if (sizeof(T) == 4)
-      fis = fis * (T)inverse_k_f;
+      fis = mul_rn(fis, (T)inverse_k_f);
     else
       fis = fis / (T)keff;
     if (WITH_KEFF) {
@@ -157,7 +167,7 @@ __global__ void __launch_bounds__(RTHREADS) update_kernel(
     // scatter source and new source per group (src/solver.c:1274-1300)
     for (int g = lane; g < G; g += 32) {
       T sc = 0;
-      for (int g2 = 0; g2 < G; ++g2) sc += (T)S[(int64_t)g2 * G + g] * myphi[g2];
+      for (int g2 = 0; g2 < G; ++g2) sc = add_rn(sc, mul_rn((T)S[(int64_t)g2 * G + g], myphi[g2]));
       const T chi = (T)x[g * 3 + 2];
       T nw;
       if (sizeof(T) == 4)
@@ -165,8 +175,8 @@ __global__ void __launch_bounds__(RTHREADS) update_kernel(
       else
         nw = (fis * chi + sc) / (T)(4.0 * PI);
       const T old = qr[g];
-      const T d = nw - old;
-      res_acc += (double)(d * d / (old * old));
+      const T d = add_rn(nw, -old);
+      res_acc += (double)div_rn(mul_rn(d, d), mul_rn(old, old));
       qr[g] = nw;
     }
     __syncwarp();
