@@ -58,7 +58,7 @@ class ProblemSpec:
         return self.n_tracks_3d * self.n_seg * self.n_groups
 
     def algorithmic_bytes(self) -> int:
-        """HBM bytes one sweep must move at minimum (see DESIGN.md):
+        """HBM bytes one sweep must move at minimum:
         3 fine-source rows read + tally read-modify-write per integration
         (20 B), psi read + write per track-group (8 B), 3D segment stream
         (source id, 4 B per segment) and 3D lengths (4 B per 2D segment and
@@ -92,7 +92,11 @@ CONFIG_DEFAULT = ProblemSpec(
     n_groups=100, fai=5, cai=6, height=400.0, n_sources=pins(17, 17) * 6,
     n_tracks_2d=64 * 256, n_polar=10, z_stacked=80, n_seg=50, seed=20260102)
 
-CONFIGS = {"small": CONFIG_SMALL, "default": CONFIG_DEFAULT}
+# The default problem's full source storage (2 GB of FSR arrays, larger than
+# L2) swept by 1024 of its 16384 2D tracks: the profiling case (~3 GB).
+CONFIG_DEFAULT_1K = CONFIG_DEFAULT.with_(n_tracks_2d=1024)
+
+CONFIGS = {"small": CONFIG_SMALL, "default": CONFIG_DEFAULT, "default_1k": CONFIG_DEFAULT_1K}
 
 
 def exp_table(precision: float, maxval: float = 10.0):
