@@ -514,7 +514,8 @@ int64_t oracle_sweep64(const oracle_problem *P, const double *fine_source,
     int j = (int)((t / P->Z) % P->P);
     float theta = P->polar_angles[j];
     float mu = oracle_mu(theta);
-    double weight = (double)P->p_weight[t] * (double)P->az_weight[i];
+    /* the track weight is an input quantity: the reference's float product */
+    double weight = (double)(P->p_weight[t] * P->az_weight[i]);
     float z = P->z0[t];
     double *psi = psi_f + t * G;
     for (int64_t n = 0; n < S; n++) {

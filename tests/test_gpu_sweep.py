@@ -112,7 +112,8 @@ def test_plain_ten_power_iterations_vs_oracle(gpu_available, port, axial_exp):
 
 def test_power_iteration_equals_separate_calls(gpu_available):
     """moc_power_iteration (fused update + keff) and the four separate calls
-    give the same state (same kernels, same order)."""
+    give the same results; two sweeps differ only in the order of their FP32
+    tally additions, so the comparison is to rounding."""
     import simplemoc_gb300 as sm
     hp = sm.generate(_spec(n_tracks_2d=16, z_stacked=10))
     with _solver(hp) as a, _solver(hp) as b:
@@ -122,9 +123,10 @@ def test_power_iteration_equals_separate_calls(gpu_available):
         rb = b.update_sources(1.0)
         kb = b.compute_keff(0.0)
         oa, ob = a.download(), b.download()
-    assert ra == rb
-    assert ka == kb
+    assert abs(ra - rb) <= 1e-6 * abs(rb)
+    assert abs(ka - kb) <= 1e-7 * abs(kb)
     assert rel_err(oa["fine_flux"], ob["fine_flux"]) <= PHI_TOL
+    assert rel_err(oa["fine_source"], ob["fine_source"]) <= PHI_TOL
 
 
 @pytest.mark.parametrize("axial_exp", [2, 0])
