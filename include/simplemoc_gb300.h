@@ -192,6 +192,31 @@ int moc_time_power_iterations(moc_problem *p, int iters, double *ms_total,
 /* Number of kernels the library has launched on this handle so far. */
 int64_t moc_launch_count(const moc_problem *p);
 
+/* ---- renormalize_flux without device allocation ------------------------ */
+/* No counterpart in the reference.  For callers that cannot let the library
+ * call cudaMalloc (a framework or pool allocator that accounts for every
+ * device byte, a real-time loop that allocates nothing after start-up,
+ * buffers mapped from another process): the same computation as
+ * moc_renormalize_flux on device buffers the caller owns, in the reference
+ * layout (row stride n_groups):
+ *   fine_flux [n_sources*fai*n_groups]  in/out   psi_f, psi_b [n_tracks_3d*n_groups] in/out
+ *   vol [n_sources], src_xs [n_sources], xs [n_xs*n_groups*3]  in
+ *   norm_out: NULL or a device double[2] receiving (total fission rate, norm)
+ * Launches on `stream` (a cudaStream_t; NULL = the legacy default stream) and
+ * returns without waiting.  Its scratch is a static device array of
+ * MOC_NOALLOC_SCRATCH_BYTES reserved on every GPU that loads the library until
+ * the process exits; n_sources above MOC_NOALLOC_MAX_SOURCES is rejected with
+ * MOC_ERR_ARG.  The first call on a device looks up the array's device address
+ * (make it before any stream capture).  All calls share the one array: calls
+ * whose kernels overlap on the GPU race. */
+#define MOC_NOALLOC_MAX_SOURCES (1 << 20)
+#define MOC_NOALLOC_SCRATCH_BYTES (8 * 1032 + 4 * MOC_NOALLOC_MAX_SOURCES)
+int moc_renormalize_flux_noalloc(float *fine_flux, float *psi_f, float *psi_b,
+                                 const float *vol, const int32_t *src_xs,
+                                 const float *xs, int64_t n_sources, int32_t fai,
+                                 int32_t n_groups, int64_t n_tracks_3d,
+                                 double *norm_out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

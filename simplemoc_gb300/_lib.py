@@ -97,6 +97,9 @@ SIGNATURES = {
     "moc_time_sweep": (C.c_int, [C.c_void_p, C.c_int, f64p]),
     "moc_launch_count": (C.c_int64, [C.c_void_p]),
     "moc_time_power_iterations": (C.c_int, [C.c_void_p, C.c_int, f64p, f64p, f64p, f64p]),
+    "moc_renormalize_flux_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                               C.c_void_p, C.c_void_p, C.c_int64, C.c_int32,
+                                               C.c_int32, C.c_int64, C.c_void_p, C.c_void_p]),
 }
 
 _LIB: C.CDLL | None = None

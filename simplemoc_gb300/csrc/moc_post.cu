@@ -11,6 +11,8 @@
 #include <math.h>
 #include <stdint.h>
 
+#include <mutex>
+
 #include "moc_internal.h"
 
 namespace {
@@ -323,5 +325,97 @@ int moc_set_leakage(moc_problem *p, double leakage) {
   set_scalar<<<1, 1, 0, p->stream>>>(p->scalars, SC_LEAKAGE, leakage);
   p->launches++;
   MOC_CUDA_TRY(cudaGetLastError());
+  return MOC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// renormalize_flux without device allocation.
+//
+// Some callers cannot let a library call cudaMalloc: a framework or memory
+// pool that must account for every device byte it hands out, a real-time loop
+// that forbids allocation once it has started, or a process whose buffers are
+// mapped from another process over IPC.  This entry point runs the same four
+// kernels as moc_renormalize_flux on buffers the caller owns, with its scratch
+// (per-block partial sums, the two scalars, one float per source region) in a
+// file-scope device array instead of an allocation.  The array is reserved on
+// every GPU that loads the library and stays there until the process exits.
+//
+// Host code must not pass g_renorm_scratch itself to a kernel: on the host the
+// name is only a stand-in for the device object.  Its device address is looked
+// up once per device with cudaGetSymbolAddress, below, while that device is
+// current; the first call on a device does this set-up, so make that first
+// call before any stream capture.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr int64_t NOALLOC_FLOATS = MOC_NOALLOC_MAX_SOURCES;                 // adjust[]
+constexpr int64_t NOALLOC_DOUBLES = RBLOCKS + SC_COUNT + NOALLOC_FLOATS / 2;
+
+static __device__ __align__(256) double g_renorm_scratch[NOALLOC_DOUBLES];
+static_assert(sizeof(g_renorm_scratch) == MOC_NOALLOC_SCRATCH_BYTES,
+              "scratch size must match the size stated in the header");
+
+constexpr int NOALLOC_MAX_DEVICES = 64;
+std::mutex g_scratch_mu;
+double *g_scratch_dev[NOALLOC_MAX_DEVICES] = {};
+
+// Device address of g_renorm_scratch on the current device (set-up once).
+int scratch_address(int device, double **out) {
+  std::lock_guard<std::mutex> lock(g_scratch_mu);
+  if (!g_scratch_dev[device]) {
+    void *ptr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&ptr, g_renorm_scratch);
+    if (e != cudaSuccess || ptr == nullptr) {
+      cudaGetLastError();
+      return MOC_ERR_CUDA;
+    }
+    g_scratch_dev[device] = static_cast<double *>(ptr);
+  }
+  *out = g_scratch_dev[device];
+  return MOC_OK;
+}
+
+}  // namespace
+
+extern "C" int moc_renormalize_flux_noalloc(float *fine_flux, float *psi_f, float *psi_b,
+                                            const float *vol, const int32_t *src_xs,
+                                            const float *xs, int64_t n_sources, int32_t fai,
+                                            int32_t n_groups, int64_t n_tracks_3d,
+                                            double *norm_out, void *stream) {
+  if (!fine_flux || !psi_f || !psi_b || !vol || !src_xs || !xs) return MOC_ERR_ARG;
+  if (n_sources < 1 || fai < 1 || n_groups < 1 || n_tracks_3d < 0) return MOC_ERR_ARG;
+  if (n_sources > MOC_NOALLOC_MAX_SOURCES) return MOC_ERR_ARG;   // scratch holds one float per source
+  int device = 0;
+  if (cudaGetDevice(&device) != cudaSuccess) {
+    cudaGetLastError();
+    return MOC_ERR_NO_DEVICE;
+  }
+  if (device < 0 || device >= NOALLOC_MAX_DEVICES) return MOC_ERR_UNSUPPORTED;
+  double *scratch = nullptr;
+  int rc = scratch_address(device, &scratch);
+  if (rc != MOC_OK) return rc;
+  double *partials = scratch;
+  double *scalars = scratch + RBLOCKS;
+  float *adjust = reinterpret_cast<float *>(scratch + RBLOCKS + SC_COUNT);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const int64_t nfsr = n_sources * fai;
+  int sms = 0;
+  MOC_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+  // Every scratch slot read below is written earlier in the same call (all
+  // RBLOCKS partials, both scalars, adjust[0..n_sources)), so nothing has to be
+  // cleared between calls.  Two calls whose kernels overlap on the GPU (other
+  // streams, other host threads) share the one array and race.
+  renorm_partials<float><<<RBLOCKS, RTHREADS, 0, s>>>(fine_flux, vol, src_xs, xs, nfsr, fai,
+                                                      n_groups, n_groups, partials);
+  renorm_finalize<float><<<1, 32, 0, s>>>(partials, RBLOCKS, scalars);
+  renorm_adjust<float><<<(unsigned)((n_sources + 255) / 256), 256, 0, s>>>(vol, n_sources, fai,
+                                                                           scalars, adjust);
+  renorm_scale<float><<<(unsigned)(sms * 8), RTHREADS, 0, s>>>(
+      fine_flux, adjust, nfsr * n_groups, (int64_t)fai * n_groups, psi_f, psi_b,
+      n_tracks_3d * n_groups, scalars);
+  MOC_CUDA_TRY(cudaGetLastError());
+  if (norm_out)
+    MOC_CUDA_TRY(cudaMemcpyAsync(norm_out, scalars + SC_TOTAL_FISSION, 2 * sizeof(double),
+                                 cudaMemcpyDeviceToDevice, s));
   return MOC_OK;
 }
