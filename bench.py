@@ -255,6 +255,7 @@ def main():
     ints = spec.integrations_per_sweep
 
     # ---- chosen (MIXED) ------------------------------------------------------
+    shapes = {"mixed": list(solver.autotune()[:2])}
     if W:
         solver.time_power_iterations(W)
     barrier()
@@ -273,11 +274,13 @@ def main():
 
     # ---- plain (reference arithmetic) ------------------------------------------
     solver.set_mode("plain")
+    shapes["plain"] = list(solver.autotune()[:2])
     solver.time_power_iterations(1)
     rp = solver.time_power_iterations(K)
     plain_value = ints * K / (rp["ms_total"] / 1e3)
     plain_sweep_ms = rp["ms_sweeps"] / K
     solver.set_mode("mixed")
+    solver.autotune(measure=False)
 
     # ---- end to end through the C ABI with host buffers ------------------------
     e2e = None
@@ -349,7 +352,7 @@ def main():
             "plain": {"value": plain_value, "unit": "integrations/s",
                       "sweep_ms": plain_sweep_ms},
             "chosen_vs_plain": value / world / plain_value,
-            "sweep_ms": sweep_ms, "keff": r["keff"],
+            "sweep_ms": sweep_ms, "keff": r["keff"], "launch_shape": shapes,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
                          "peak_source": peak_kind,

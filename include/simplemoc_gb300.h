@@ -160,6 +160,15 @@ int moc_set_launch(moc_problem *p, int threads_per_track, int chunks_per_thread)
 int moc_get_launch(const moc_problem *p, int *threads_per_track,
                    int *chunks_per_thread);
 
+/* Autotuner: times every launch shape of the current mode on the first
+ * n_tracks tracks (0 = up to 262144), with scratch tally and angular-flux
+ * buffers so that the problem's state is unchanged, and selects the fastest.
+ * Choices are cached per (segments per track, groups, polar angles, mode,
+ * source order, compensation); with ms_best == NULL a cached choice is reused
+ * without timing. */
+int moc_autotune(moc_problem *p, int64_t n_tracks, int *threads_per_track,
+                 int *chunks_per_thread, double *ms_best);
+
 /* ---- the hot path (replaces src/solver.c) ------------------------------- */
 /* transport_sweep (src/solver.c:283-552) over the explicit 3D tracks:
  * attenuates every segment, tallies fine_flux, updates psi_f in place.

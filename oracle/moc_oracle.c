@@ -326,6 +326,93 @@ int64_t oracle_sweep_omp(const oracle_problem *P, const float *fine_source,
 }
 
 /* ------------------------------------------------------------------------ */
+/* the reference traversal, src/solver.c:283-552 (serial build)              */
+/* ------------------------------------------------------------------------ */
+/* src/solver.c:895-907: float z, float dz */
+static int pos_interval(float z, float dz) { return (int)(z / dz); }
+static int neg_interval(float z, float dz) { return ceil(z / dz); }
+
+int64_t oracle_ref_sweep(const oracle_problem *P, const oracle_refgeo *R,
+                         const float *fine_source, float *fine_flux, float *psi_f,
+                         float *z_height, const int32_t *ids)
+{
+  const int64_t G = P->G, F = P->F, NS = P->NS;
+  /* solver.c:288-289: float height / int -> float, held in double */
+  double node_delta_z = P->height / P->decomp_ax;
+  double fine_delta_z = node_delta_z / (P->cai * P->F);
+  int64_t seq = 0;
+  for (int64_t i = 0; i < R->N2D; i++) {                       /* solver.c:348 */
+    int pos_z_dir = 1;
+    const int64_t nseg = R->seg_off[i + 1] - R->seg_off[i];
+    const float *len = R->seg_len + R->seg_off[i];
+    for (int j = 0; j < P->P; j++) {                           /* solver.c:368 */
+      if (j == P->P / 2)
+        pos_z_dir = 0;
+      float p_angle = P->polar_angles[j];
+      float mu = cos(p_angle);
+      int begin_stacked = 0;
+      int end_stacked = P->Z;
+      for (int64_t n = 0; n < nseg; n++) {                     /* solver.c:379 */
+        float s_full = len[n] / sin(p_angle);
+        float ds = 0;
+        for (int k = begin_stacked; k < end_stacked; k++) {    /* solver.c:389 */
+          float s = s_full;
+          const int64_t t = ((int64_t)i * P->P + j) * P->Z + k;
+          int seg_complete = 0;
+          int curr_interval = pos_z_dir ? pos_interval(z_height[t], fine_delta_z)
+                                        : neg_interval(z_height[t], fine_delta_z);
+          while (!seg_complete) {                              /* solver.c:409 */
+            int reset = 0;
+            float z = z_height[t] + s * cos(p_angle);
+            int new_interval = pos_z_dir ? pos_interval(z, fine_delta_z)
+                                         : neg_interval(z, fine_delta_z);
+            if (new_interval == curr_interval) {
+              seg_complete = 1;
+              ds = s;
+            } else {
+              if (pos_z_dir) {
+                curr_interval++;
+                z = fine_delta_z * (float)curr_interval;
+              } else {
+                curr_interval--;
+                z = fine_delta_z * (float)curr_interval;
+              }
+              ds = (z - z_height[t]) / cos(p_angle);
+              s -= ds;
+              if (s <= 0)
+                seg_complete = 1;
+              if (z <= 0 || z >= node_delta_z) {               /* solver.c:460-473 */
+                seg_complete = 1;
+                if (pos_z_dir)
+                  end_stacked--;
+                else
+                  begin_stacked++;
+                reset = 1;
+              }
+            }
+            int64_t qsr = ids ? ids[seq] : (int64_t)(rand() % NS);   /* solver.c:481 */
+            seq++;
+            float weight = R->p_weight[t] * R->az_weight[i];
+            oracle_attenuate(P, z_height[t], ds, mu, weight, fine_source + qsr * F * G,
+                             fine_flux + qsr * F * G, P->sigt + (int64_t)P->src_sigt[qsr] * G,
+                             psi_f + t * G);
+            if (n == nseg - 1 || reset) {                      /* solver.c:514-523 */
+              if (pos_z_dir)
+                z_height[t] = R->axial_z_sep * k;
+              else
+                z_height[t] = R->axial_z_sep * (k + 1);
+            } else {
+              z_height[t] = z;
+            }
+          }
+        }
+      }
+    }
+  }
+  return seq;
+}
+
+/* ------------------------------------------------------------------------ */
 /* post-sweep steps, serial build semantics                                  */
 /* ------------------------------------------------------------------------ */
 void oracle_renormalize(const oracle_problem *P, float *fine_flux,

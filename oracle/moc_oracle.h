@@ -85,6 +85,26 @@ int64_t oracle_sweep_omp(const oracle_problem *P, const float *fine_source,
 /* Threads OpenMP will use (0 when built without OpenMP). */
 int     oracle_omp_max_threads(void);
 
+/* The reference's own traversal (src/solver.c:347-523, serial build): 2D
+ * tracks with their own segment counts, the z-stacked rays of each polar
+ * angle, axial splitting at fine-interval boundaries, the begin/end retirement
+ * of stacked rays at the domain bounds, and the stacked-ray height state kept
+ * between sweeps.  The source region of each 3D sub-segment is ids[seq] for the
+ * seq-th sub-segment in traversal order, or rand() % NS (libc, exactly as the
+ * serial reference) when ids is NULL. */
+typedef struct oracle_refgeo {
+  int64_t N2D;
+  const int64_t *seg_off;      /* [N2D+1] first segment of each 2D track */
+  const float *seg_len;        /* [seg_off[N2D]] 2D segment lengths */
+  const float *az_weight;      /* [N2D] */
+  const float *p_weight;       /* [N3D] */
+  float axial_z_sep;           /* Input.axial_z_sep */
+} oracle_refgeo;
+
+int64_t oracle_ref_sweep(const oracle_problem *P, const oracle_refgeo *R,
+                         const float *fine_source, float *fine_flux, float *psi_f,
+                         float *z_height, const int32_t *ids);
+
 /* src/solver.c:1143-1230, serial build semantics. */
 void  oracle_renormalize(const oracle_problem *P, float *fine_flux,
                          float *psi_f, float *psi_b);

@@ -34,8 +34,13 @@ static AttenuateVars A;
 static float *A_buf;
 static float leak;
 
+static Track2D *tracks2d;
+static Segment *segs2d;
+
 void refh_teardown(void)
 {
+  free(tracks2d); free(segs2d);
+  tracks2d = NULL; segs2d = NULL;
   free(src); free(track_data); free(track_rows); free(tracks);
   free(fs_rows); free(ff_rows); free(xs_rows); free(sc_rows); free(A_buf);
   if (Pr.expTable.values) free(Pr.expTable.values);
@@ -168,6 +173,42 @@ long refh_sweep(void)
   }
   I.segments_processed = segments;
   return segments;
+}
+
+/* ---- the reference's own transport_sweep over a reference-style geometry --- */
+
+/* Fills Params.tracks_2D (2D tracks with their own segment counts) and the
+ * stacked-ray heights, on top of a refh_setup() problem. */
+int refh_setup_ref(const oracle_refgeo *R, const float *z_height, float axial_z_sep)
+{
+  free(tracks2d); free(segs2d);
+  const long N2D = R->N2D;
+  tracks2d = calloc(N2D, sizeof(Track2D));
+  segs2d = calloc(R->seg_off[N2D] > 0 ? R->seg_off[N2D] : 1, sizeof(Segment));
+  for (long i = 0; i < N2D; i++) {
+    tracks2d[i].az_weight = R->az_weight[i];
+    tracks2d[i].n_segments = R->seg_off[i + 1] - R->seg_off[i];
+    tracks2d[i].segments = &segs2d[R->seg_off[i]];
+    for (long n = 0; n < tracks2d[i].n_segments; n++)
+      tracks2d[i].segments[n].length = R->seg_len[R->seg_off[i] + n];
+  }
+  Pr.tracks_2D = tracks2d;
+  I.axial_z_sep = axial_z_sep;
+  for (long t = 0; t < I.ntracks; t++) {
+    track_data[t].z_height = z_height[t];
+    track_data[t].p_weight = R->p_weight[t];
+  }
+  return 0;
+}
+
+/* The reference's transport_sweep (src/solver.c:283-552, serial build: the
+ * source regions come from libc rand(), seeded by the caller's srand). */
+long refh_transport_sweep(float *z_height_out)
+{
+  transport_sweep(&Pr, &I);
+  for (long t = 0; t < I.ntracks; t++)
+    z_height_out[t] = track_data[t].z_height;
+  return I.segments_processed;
 }
 
 void refh_renormalize(void)

@@ -88,6 +88,8 @@ SIGNATURES = {
     "moc_set_mode": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "moc_set_launch": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "moc_get_launch": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "moc_autotune": (C.c_int, [C.c_void_p, C.c_int64, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                               f64p]),
     "moc_transport_sweep": (C.c_int, [C.c_void_p, i64p]),
     "moc_renormalize_flux": (C.c_int, [C.c_void_p]),
     "moc_update_sources": (C.c_int, [C.c_void_p, C.c_double, f64p]),

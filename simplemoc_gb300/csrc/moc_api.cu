@@ -107,6 +107,21 @@ int upload_all(moc_problem *p, const moc_host *h) {
   // one wrap per segment keeps the height rule exact (checked, not assumed)
   const float hd = d.height / (float)d.decomp_ax;
   if (!(max_step < hd)) return MOC_ERR_ARG;
+  // zi % F as zi - F * umulhi(zi, m): verified for every fine-interval index
+  // the heights can reach (start heights and one wrap of [0, hd)).
+  {
+    float zmax = hd;
+    for (int64_t t = 0; t < p->n3d; ++t) zmax = h->z0[t] > zmax ? h->z0[t] : zmax;
+    const float dz = d.height / (float)(d.fai * d.decomp_ax * d.cai);
+    const double lim = (double)zmax / (double)dz + 4.0;
+    uint32_t m = (uint32_t)(0x100000000ull / (uint64_t)d.fai + 1ull);
+    if (lim > (double)(1u << 24)) m = 0;
+    for (uint32_t zi = 0; m && zi <= (uint32_t)lim; ++zi) {
+      const uint32_t q = (uint32_t)(((uint64_t)zi * m) >> 32);
+      if (zi - q * (uint32_t)d.fai != zi % (uint32_t)d.fai) m = 0;
+    }
+    p->fmagic = m;
+  }
   TRY(put(p, p->seg_ds, seg_ds.data(), N2D * P * S));
   TRY(put(p, p->seg_src, h->seg_src, p->n3d * S));
   TRY(put(p, p->weight, weight.data(), p->n3d));
@@ -119,6 +134,27 @@ int upload_all(moc_problem *p, const moc_host *h) {
   TRY(put(p, p->xs, h->xs, (int64_t)d.n_xs * G * 3));
   TRY(put(p, p->scatter_t, st.data(), (int64_t)st.size()));
   TRY(put(p, p->table, h->table, 2 * (int64_t)d.table_n));
+  // update_sources work list: sources grouped by xs row, items of <= 128 sources
+  {
+    std::vector<int64_t> start((size_t)d.n_xs + 1, 0);
+    for (int64_t s = 0; s < NS; ++s) start[(size_t)h->src_xs[s] + 1]++;
+    for (int32_t m = 0; m < d.n_xs; ++m) start[(size_t)m + 1] += start[(size_t)m];
+    std::vector<int32_t> order((size_t)NS), items;
+    std::vector<int64_t> fill(start.begin(), start.end() - 1);
+    for (int64_t s = 0; s < NS; ++s) order[(size_t)fill[(size_t)h->src_xs[s]]++] = (int32_t)s;
+    for (int32_t m = 0; m < d.n_xs; ++m)
+      for (int64_t a = start[(size_t)m]; a < start[(size_t)m + 1]; a += 128) {
+        const int64_t b = a + 128 < start[(size_t)m + 1] ? a + 128 : start[(size_t)m + 1];
+        items.push_back(m);
+        items.push_back((int32_t)a);
+        items.push_back((int32_t)b);
+      }
+    p->n_upd_items = (int32_t)(items.size() / 3);
+    TRY(put(p, p->xs_order, order.data(), NS));
+    TRY(put(p, p->upd_items, items.data(), (int64_t)items.size()));
+    // the pageable sources above must be consumed before the vectors go away
+    MOC_CUDA_TRY(cudaStreamSynchronize(p->stream));
+  }
   TRY(put_rows(p, p->q, h->fine_source, p->nfsr));
   TRY(put_rows(p, p->phi, h->fine_flux, p->nfsr));
   TRY(put_rows(p, p->psi_f, h->psi_f, p->n3d));
@@ -133,6 +169,8 @@ int upload_all(moc_problem *p, const moc_host *h) {
     widen_kernel<<<1024, 256, 0, p->stream>>>(p->psi_b, p->psi_b64, p->n3d * p->ldg);
     p->launches += 4;
   }
+  p->psi_pending = false;
+  TRY(moc_detect_psi_b(p));
   MOC_CUDA_TRY(cudaMemsetAsync(p->err, 0, sizeof(int32_t), p->stream));
   return MOC_OK;
 }
@@ -143,6 +181,7 @@ void release(moc_problem *p) {
   dfree(p->scatter_t); dfree(p->table); dfree(p->q); dfree(p->phi); dfree(p->phi_lo);
   dfree(p->psi_f); dfree(p->psi_b); dfree(p->q64); dfree(p->phi64); dfree(p->psi_f64);
   dfree(p->psi_b64); dfree(p->partials); dfree(p->scalars); dfree(p->err);
+  dfree(p->xs_order); dfree(p->upd_items); dfree(p->psi_scale); dfree(p->psi_b_nonzero);
   if (p->ev0) cudaEventDestroy(p->ev0);
   if (p->ev1) cudaEventDestroy(p->ev1);
   if (p->stream) cudaStreamDestroy(p->stream);
@@ -184,6 +223,7 @@ int read_scalars(moc_problem *p, double *out) {
 int sweep_impl(moc_problem *p) {
   int rc = moc_launch_sweep(p);
   if (rc != MOC_OK) return fail(p, rc);
+  if (p->mode != MOC_MODE_FP64) p->psi_pending = false;   // the sweep applied it
   if (p->mode == MOC_MODE_MIXED && (p->flags & MOC_FLAG_COMPENSATED) && p->phi_lo) {
     fold_kernel<<<1024, 256, 0, p->stream>>>(p->phi, p->phi_lo, p->nfsr * p->ldg);
     p->launches++;
@@ -247,6 +287,10 @@ int moc_create(const moc_dims *dims, const moc_host *host, int device, moc_probl
   if (rc == MOC_OK) rc = dalloc(p, &p->xs, (int64_t)dims->n_xs * G * 3);
   if (rc == MOC_OK) rc = dalloc(p, &p->scatter_t, (int64_t)dims->n_xs * G * G);
   if (rc == MOC_OK) rc = dalloc(p, &p->table, 2 * (int64_t)dims->table_n);
+  if (rc == MOC_OK) rc = dalloc(p, &p->xs_order, NS);
+  if (rc == MOC_OK) rc = dalloc(p, &p->psi_scale, 1);
+  if (rc == MOC_OK) rc = dalloc(p, &p->psi_b_nonzero, 1);
+  if (rc == MOC_OK) rc = dalloc(p, &p->upd_items, 3 * ((int64_t)dims->n_xs + NS / 128 + 1));
   if (rc == MOC_OK) rc = dalloc(p, &p->q, p->nfsr * p->ldg);
   if (rc == MOC_OK) rc = dalloc(p, &p->phi, p->nfsr * p->ldg);
   if (rc == MOC_OK) rc = dalloc(p, &p->psi_f, p->n3d * p->ldg);
@@ -295,6 +339,10 @@ int moc_upload(moc_problem *p, const moc_host *host) {
 int moc_download(moc_problem *p, float *fine_flux, float *fine_source, float *psi_f, float *psi_b) {
   int rc = usable(p);
   if (rc != MOC_OK) return rc;
+  if (psi_f && p->psi_pending) {
+    rc = moc_psi_materialize(p);
+    if (rc != MOC_OK) return fail(p, rc);
+  }
   rc = sync_check(p);
   if (rc != MOC_OK) return rc;
   if (fine_flux) rc = get_rows(p, fine_flux, p->phi, p->nfsr);
@@ -331,6 +379,10 @@ int moc_set_mode(moc_problem *p, int mode, int flags) {
   if (rc != MOC_OK) return rc;
   if (mode != MOC_MODE_PLAIN && mode != MOC_MODE_MIXED && mode != MOC_MODE_FP64) return MOC_ERR_ARG;
   if (flags & ~MOC_FLAG_COMPENSATED) return MOC_ERR_ARG;
+  if (p->psi_pending) {
+    rc = moc_psi_materialize(p);
+    if (rc != MOC_OK) return fail(p, rc);
+  }
   if (mode == MOC_MODE_FP64 && !p->q64) {
     // the FP64 state starts from the current FP32 state
     rc = dalloc(p, &p->q64, p->nfsr * p->ldg);
@@ -381,6 +433,21 @@ int moc_set_launch(moc_problem *p, int threads_per_track, int chunks_per_thread)
 int moc_get_launch(const moc_problem *p, int *threads_per_track, int *chunks_per_thread) {
   if (!p || !threads_per_track || !chunks_per_thread) return MOC_ERR_ARG;
   return moc_sweep_launch_shape(p, threads_per_track, chunks_per_thread);
+}
+
+int moc_autotune(moc_problem *p, int64_t n_tracks, int *threads_per_track,
+                 int *chunks_per_thread, double *ms_best) {
+  int rc = usable(p);
+  if (rc != MOC_OK) return rc;
+  cudaSetDevice(p->device);
+  int tpw = 0, cpl = 0;
+  rc = moc_sweep_autotune(p, n_tracks, &tpw, &cpl, ms_best);
+  if (rc != MOC_OK) return rc;
+  p->tpw = tpw;
+  p->cpl = cpl;
+  if (threads_per_track) *threads_per_track = tpw;
+  if (chunks_per_thread) *chunks_per_thread = cpl;
+  return MOC_OK;
 }
 
 int moc_transport_sweep(moc_problem *p, int64_t *segments_processed) {

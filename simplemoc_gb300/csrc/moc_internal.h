@@ -27,6 +27,7 @@ struct SweepArgs {
   float *phi;               // [NS*F*ldg]
   float *phi_lo;            // [NS*F*ldg] compensation words (MIXED + flag) or null
   float *psi;               // [N3D*ldg]  forward angular flux, in place
+  const float *psi_scale;   // pending renormalisation factor of psi, or null
   const double *q64;        // FP64 mode state
   double *phi64;
   double *psi64;
@@ -40,6 +41,7 @@ struct SweepArgs {
   float dz, rdz;            // fine interval height and its reciprocal
   float d1, rd1, d2, rd2;   // 2 dz and 2 dz dz, and reciprocals
   float hd;                 // domain height
+  uint32_t fmagic;          // zi % F == zi - F*umulhi(zi, fmagic) for reachable zi; 0 = use %
   int32_t *err;             // device error word (0 = ok)
 };
 
@@ -54,6 +56,7 @@ struct moc_problem {
   int64_t launches = 0;
   int64_t n3d = 0, nfsr = 0;
   int32_t ldg = 0;
+  uint32_t fmagic = 0;
   int64_t bytes = 0;
   // inputs
   float *seg_ds = nullptr;
@@ -65,6 +68,17 @@ struct moc_problem {
   // state
   float *q = nullptr, *phi = nullptr, *phi_lo = nullptr, *psi_f = nullptr, *psi_b = nullptr;
   double *q64 = nullptr, *phi64 = nullptr, *psi_f64 = nullptr, *psi_b64 = nullptr;
+  // update_sources work list: sources ordered by xs row, and items
+  // (xs row, first, end) of at most 128 sources each, over that order
+  int32_t *xs_order = nullptr;
+  int32_t *upd_items = nullptr;
+  int32_t n_upd_items = 0;
+  // lazy psi renormalisation (FP32 modes): psi_f holds values still to be
+  // multiplied by *psi_scale while psi_pending; psi_b is scaled only when the
+  // device flag psi_b_nonzero is set
+  float *psi_scale = nullptr;
+  int32_t *psi_b_nonzero = nullptr;
+  bool psi_pending = false;
   // reductions / scalars
   double *partials = nullptr;    // [3 * RED_BLOCKS]
   double *scalars = nullptr;     // see post kernels
@@ -78,11 +92,14 @@ struct moc_problem {
 // Launchers implemented in moc_sweep.cu / moc_post.cu.
 int moc_launch_sweep(moc_problem *p);
 int moc_sweep_launch_shape(const moc_problem *p, int *tpw, int *cpl);
+int moc_sweep_autotune(moc_problem *p, int64_t n_sub, int *tpw, int *cpl, double *ms);
 int moc_launch_renormalize(moc_problem *p);
 int moc_launch_update(moc_problem *p, double keff, bool keff_on_device, bool with_keff);
 int moc_set_leakage(moc_problem *p, double leakage);
 int moc_launch_keff(moc_problem *p, double leakage);
 int moc_post_scratch_blocks();
+int moc_psi_materialize(moc_problem *p);
+int moc_detect_psi_b(moc_problem *p);
 
 // Scalars slots in p->scalars (double):
 enum {

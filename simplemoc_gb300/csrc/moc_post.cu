@@ -41,7 +41,11 @@ __device__ __forceinline__ double block_sum(double v, double *sh) {
 }
 
 // ---- renormalize_flux, step 1: fission-rate partials, sum of phi*vol*nuSigF
-// (src/solver.c:1160-1175; the float products keep the reference order).
+// (src/solver.c:1160-1175; the float products keep the reference order).  One
+// warp per fine region; each lane adds its groups in FP32 and folds the result
+// into its FP64 accumulator once per region (FP64 arithmetic is a small
+// fraction of FP32 throughput on this part, so it is kept per region, not per
+// element).
 template <typename T>
 __global__ void __launch_bounds__(RTHREADS) renorm_partials(const T *__restrict__ phi,
                                                             const float *__restrict__ vol,
@@ -51,18 +55,20 @@ __global__ void __launch_bounds__(RTHREADS) renorm_partials(const T *__restrict_
                                                             double *__restrict__ partials) {
   __shared__ double sh[RTHREADS / 32];
   double acc = 0.0;
-  const int64_t n = nfsr * (int64_t)G;
-  for (int64_t e = (int64_t)blockIdx.x * RTHREADS + threadIdx.x; e < n;
-       e += (int64_t)gridDim.x * RTHREADS) {
-    const int64_t row = e / G;
-    const int g = (int)(e - row * G);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int64_t row = (int64_t)blockIdx.x * (RTHREADS / 32) + warp; row < nfsr;
+       row += (int64_t)gridDim.x * (RTHREADS / 32)) {
     const int64_t s = row / F;
-    const float nusf = xs[((int64_t)src_xs[s] * G + g) * 3 + 0];
+    const float v_s = vol[s];
+    const float *x = xs + (int64_t)src_xs[s] * G * 3;
+    const T *ph = phi + row * ldg;
     if (sizeof(T) == 4) {
-      float v = __fmul_rn(__fmul_rn((float)phi[row * ldg + g], vol[s]), nusf);
-      acc += (double)v;
+      float r = 0.f;
+      for (int g = lane; g < G; g += 32)
+        r = __fadd_rn(r, __fmul_rn(__fmul_rn((float)ph[g], v_s), x[g * 3 + 0]));
+      acc += (double)r;
     } else {
-      acc += (double)phi[row * ldg + g] * (double)vol[s] * (double)nusf;
+      for (int g = lane; g < G; g += 32) acc += (double)ph[g] * (double)v_s * (double)x[g * 3];
     }
   }
   double b = block_sum(acc, sh);
@@ -193,7 +199,8 @@ __global__ void __launch_bounds__(RTHREADS) update_kernel(
   }
 }
 
-// compute_keff sums alone (src/solver.c:1335-1382)
+// compute_keff sums alone (src/solver.c:1335-1382): one warp per fine region,
+// FP32 within the region's groups, FP64 across regions.
 template <typename T>
 __global__ void __launch_bounds__(RTHREADS) keff_partials(const T *__restrict__ phi,
                                                           const int32_t *__restrict__ src_xs,
@@ -202,15 +209,19 @@ __global__ void __launch_bounds__(RTHREADS) keff_partials(const T *__restrict__ 
                                                           double *__restrict__ partials) {
   __shared__ double sh[RTHREADS / 32];
   double ab = 0.0, fi = 0.0;
-  const int64_t n = nfsr * (int64_t)G;
-  for (int64_t e = (int64_t)blockIdx.x * RTHREADS + threadIdx.x; e < n;
-       e += (int64_t)gridDim.x * RTHREADS) {
-    const int64_t row = e / G;
-    const int g = (int)(e - row * G);
-    const float *x = xs + ((int64_t)src_xs[row / F] * G + g) * 3;
-    const T v = phi[row * ldg + g];
-    ab += (double)((T)x[1] * v);
-    fi += (double)((T)x[0] * v);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int64_t row = (int64_t)blockIdx.x * (RTHREADS / 32) + warp; row < nfsr;
+       row += (int64_t)gridDim.x * (RTHREADS / 32)) {
+    const float *x = xs + (int64_t)src_xs[row / F] * G * 3;
+    const T *ph = phi + row * ldg;
+    T ra = 0, rf = 0;
+    for (int g = lane; g < G; g += 32) {
+      const T v = ph[g];
+      ra = add_rn(ra, mul_rn((T)x[g * 3 + 1], v));
+      rf = add_rn(rf, mul_rn((T)x[g * 3 + 0], v));
+    }
+    ab += (double)ra;
+    fi += (double)rf;
   }
   double a = block_sum(ab, sh);
   if (threadIdx.x == 0) partials[RBLOCKS + blockIdx.x] = a;
@@ -244,6 +255,40 @@ __global__ void set_scalar(double *scalars, int slot, double v) {
   if (threadIdx.x == 0 && blockIdx.x == 0) scalars[slot] = v;
 }
 
+// Lazy angular-flux scaling (FP32 state).  renormalize_flux multiplies psi_f
+// and psi_b by norm (src/solver.c:1219-1226).  Here phi is scaled as before,
+// psi_f records a pending factor that the next sweep applies as it loads psi
+// (the same single float multiply, so PLAIN stays bit-identical), and psi_b,
+// which is never swept (src/solver.c:489), is scaled only if it holds a
+// non-zero value (a device flag set at upload).
+__global__ void __launch_bounds__(RTHREADS) renorm_scale_lazy(
+    float *__restrict__ phi, const float *__restrict__ adjust, int64_t nphi, int64_t row_elems,
+    float *__restrict__ psi_b, int64_t npsi, const int32_t *__restrict__ psi_b_nonzero,
+    const double *__restrict__ scalars, float *__restrict__ psi_scale) {
+  const float norm = (float)scalars[SC_NORM];
+  const int64_t stride = (int64_t)gridDim.x * RTHREADS;
+  const int64_t t0 = (int64_t)blockIdx.x * RTHREADS + threadIdx.x;
+  if (t0 == 0) *psi_scale = norm;
+  for (int64_t e = t0; e < nphi; e += stride) phi[e] = phi[e] * adjust[e / row_elems];
+  if (*psi_b_nonzero)
+    for (int64_t e = t0; e < npsi; e += stride) psi_b[e] = psi_b[e] * norm;
+}
+
+__global__ void psi_materialize(float *__restrict__ psi, int64_t n, const float *__restrict__ scale) {
+  const float s = *scale;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x)
+    psi[e] = psi[e] * s;
+}
+
+__global__ void detect_nonzero(const float *__restrict__ v, int64_t n, int32_t *__restrict__ flag) {
+  bool nz = false;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n;
+       e += (int64_t)gridDim.x * blockDim.x)
+    nz |= (v[e] != 0.0f);
+  if (__syncthreads_or(nz) && threadIdx.x == 0) *flag = 1;
+}
+
 template <typename T>
 int renorm_t(moc_problem *p, T *phi, T *psi_f, T *psi_b, T *adjust) {
   const moc_dims &d = p->d;
@@ -256,17 +301,174 @@ int renorm_t(moc_problem *p, T *phi, T *psi_f, T *psi_b, T *adjust) {
                                                                        p->scalars, adjust);
   int sms = 0;
   MOC_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p->device));
-  renorm_scale<T><<<(unsigned)(sms * 8), RTHREADS, 0, p->stream>>>(
-      phi, adjust, p->nfsr * p->ldg, (int64_t)d.fai * p->ldg, psi_f, psi_b, p->n3d * p->ldg,
-      p->scalars);
+  if (sizeof(T) == 4 && p->psi_scale) {
+    // a second renormalize before any sweep: apply the pending factor first so
+    // that psi sees the reference's sequence of roundings
+    if (p->psi_pending) {
+      psi_materialize<<<(unsigned)(sms * 8), RTHREADS, 0, p->stream>>>(
+          reinterpret_cast<float *>(psi_f), p->n3d * p->ldg, p->psi_scale);
+      p->launches++;
+    }
+    renorm_scale_lazy<<<(unsigned)(sms * 8), RTHREADS, 0, p->stream>>>(
+        reinterpret_cast<float *>(phi), reinterpret_cast<const float *>(adjust),
+        p->nfsr * p->ldg, (int64_t)d.fai * p->ldg, reinterpret_cast<float *>(psi_b),
+        p->n3d * p->ldg, p->psi_b_nonzero, p->scalars, p->psi_scale);
+    p->psi_pending = true;
+  } else {
+    renorm_scale<T><<<(unsigned)(sms * 8), RTHREADS, 0, p->stream>>>(
+        phi, adjust, p->nfsr * p->ldg, (int64_t)d.fai * p->ldg, psi_f, psi_b, p->n3d * p->ldg,
+        p->scalars);
+  }
   MOC_CUDA_TRY(cudaGetLastError());
   p->launches += 4;
   return MOC_OK;
 }
 
+// ---- update_sources as a material-grouped, register-tiled contraction (FP32).
+// Work item = (material m, a range of its sources).  The block stages the
+// transposed scatter matrix St_m[g2][g] of the item in shared memory; each warp
+// takes UT_ROWS fine regions at a time, stages their fluxes as [g2][row] (read
+// back as broadcasts), and every lane accumulates 4 destination groups x
+// UT_ROWS regions: acc[r][g] += St_m[g2][g] * phi_r[g2], 100 FMAs per 3 shared
+// loads.  The same pass forms the fission source and the k_eff sums; sums are
+// FP64 per block, added in block order by the finalize kernel.
+constexpr int UT_ROWS = 8;
+constexpr int UT_WARPS = RTHREADS / 32;
+
+__global__ void __launch_bounds__(RTHREADS) update_tiled_kernel(
+    const float *__restrict__ phi, float *__restrict__ q, const int32_t *__restrict__ xs_order,
+    const int32_t *__restrict__ items, int n_items, const float *__restrict__ xs,
+    const float *__restrict__ st, int F, int G, int ldg, const double *__restrict__ scalars,
+    double *__restrict__ partials) {
+  extern __shared__ float smem_f[];
+  float *sS = smem_f;                                   // [G][ldg]
+  float *sP = smem_f + (int64_t)G * ldg;                // [UT_WARPS][G][UT_ROWS]
+  __shared__ double sh[RTHREADS / 32];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float *myP = sP + (int64_t)warp * G * UT_ROWS;
+  const int nchunk = ldg / 4;
+  const float inverse_k = (float)(1.0 / scalars[SC_KEFF_IN]);     // src/solver.c:1241
+  // src/solver.c:1289-1290 divides by 4*pi in double; here the float quotient
+  // by fl(4 pi), correctly rounded (Markstein correction), within 1 ulp of it
+  const float four_pi = (float)(4.0 * PI);
+  const float r_four_pi = 1.0f / four_pi;
+  double res_acc = 0.0, abs_acc = 0.0, fis_acc = 0.0;
+  for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
+    const int m = items[3 * it], s0 = items[3 * it + 1], s1 = items[3 * it + 2];
+    const float *Sm = st + (int64_t)m * G * G;
+    const float *x = xs + (int64_t)m * G * 3;
+    __syncthreads();
+    for (int e = threadIdx.x; e < G * ldg; e += RTHREADS) {
+      const int g2 = e / ldg, g = e - g2 * ldg;
+      sS[e] = g < G ? Sm[(int64_t)g2 * G + g] : 0.f;
+    }
+    __syncthreads();
+    const int n_rows = (s1 - s0) * F;
+    for (int base = warp * UT_ROWS; base < n_rows; base += UT_WARPS * UT_ROWS) {
+      int64_t grow[UT_ROWS];
+      float fis[UT_ROWS];
+      float pa_lane = 0.f, pf_lane = 0.f;
+#pragma unroll
+      for (int r = 0; r < UT_ROWS; ++r) {
+        const int lr = base + r;
+        grow[r] = -1;
+        if (lr < n_rows) grow[r] = (int64_t)xs_order[s0 + lr / F] * F + (lr % F);
+      }
+#pragma unroll
+      for (int r = 0; r < UT_ROWS; ++r) {
+        fis[r] = 0.f;
+        for (int g = lane; g < G; g += 32) {
+          const float v = grow[r] >= 0 ? phi[grow[r] * ldg + g] : 0.f;
+          myP[g * UT_ROWS + r] = v;
+          const float fprod = __fmul_rn(v, x[g * 3 + 0]);
+          fis[r] = __fadd_rn(fis[r], fprod);
+          pa_lane = __fadd_rn(pa_lane, __fmul_rn(x[g * 3 + 1], v));
+        }
+        pf_lane = __fadd_rn(pf_lane, fis[r]);
+      }
+      abs_acc += (double)pa_lane;
+      fis_acc += (double)pf_lane;
+#pragma unroll
+      for (int r = 0; r < UT_ROWS; ++r)
+        for (int o = 16; o > 0; o >>= 1) fis[r] = __fadd_rn(fis[r], __shfl_xor_sync(0xffffffffu, fis[r], o));
+      __syncwarp();
+      if (lane < nchunk) {
+        float acc[UT_ROWS][4];
+#pragma unroll
+        for (int r = 0; r < UT_ROWS; ++r) acc[r][0] = acc[r][1] = acc[r][2] = acc[r][3] = 0.f;
+        const float *col = sS + 4 * lane;
+#pragma unroll 4
+        for (int g2 = 0; g2 < G; ++g2) {
+          const float4 s4 = *reinterpret_cast<const float4 *>(col + (int64_t)g2 * ldg);
+          const float4 pa = *reinterpret_cast<const float4 *>(myP + g2 * UT_ROWS);
+          const float4 pb = *reinterpret_cast<const float4 *>(myP + g2 * UT_ROWS + 4);
+          const float pr[UT_ROWS] = {pa.x, pa.y, pa.z, pa.w, pb.x, pb.y, pb.z, pb.w};
+#pragma unroll
+          for (int r = 0; r < UT_ROWS; ++r) {
+            acc[r][0] = fmaf(s4.x, pr[r], acc[r][0]);
+            acc[r][1] = fmaf(s4.y, pr[r], acc[r][1]);
+            acc[r][2] = fmaf(s4.z, pr[r], acc[r][2]);
+            acc[r][3] = fmaf(s4.w, pr[r], acc[r][3]);
+          }
+        }
+        float res_lane = 0.f;
+#pragma unroll
+        for (int r = 0; r < UT_ROWS; ++r) {
+          if (grow[r] < 0) continue;
+          const float fk = __fmul_rn(fis[r], inverse_k);
+          float *qr = q + grow[r] * ldg + 4 * lane;
+          float4 old = *reinterpret_cast<const float4 *>(qr);
+          float4 nw;
+          float *po = &old.x, *pn = &nw.x;
+#pragma unroll
+          for (int e = 0; e < 4; ++e) {
+            const int g = 4 * lane + e;
+            if (g < G) {
+              const float chi = x[g * 3 + 2];
+              // src/solver.c:1289-1295
+              const float num = __fadd_rn(__fmul_rn(fk, chi), acc[r][e]);
+              float qq = __fmul_rn(num, r_four_pi);
+              qq = __fmaf_rn(__fmaf_rn(-qq, four_pi, num), r_four_pi, qq);
+              pn[e] = qq;
+              const float d = __fsub_rn(pn[e], po[e]);
+              res_lane = __fadd_rn(res_lane, __fdiv_rn(__fmul_rn(d, d), __fmul_rn(po[e], po[e])));
+            } else {
+              pn[e] = po[e];
+            }
+          }
+          *reinterpret_cast<float4 *>(qr) = nw;
+        }
+        res_acc += (double)res_lane;
+      }
+      __syncwarp();
+    }
+  }
+  double r = block_sum(res_acc, sh);
+  if (threadIdx.x == 0) partials[blockIdx.x] = r;
+  double a = block_sum(abs_acc, sh);
+  if (threadIdx.x == 0) partials[RBLOCKS + blockIdx.x] = a;
+  double f = block_sum(fis_acc, sh);
+  if (threadIdx.x == 0) partials[2 * RBLOCKS + blockIdx.x] = f;
+}
+
 template <typename T>
 int update_t(moc_problem *p, const T *phi, T *q, bool with_keff) {
   const moc_dims &d = p->d;
+  if (sizeof(T) == 4 && p->upd_items && p->ldg <= 128) {
+    const size_t smem = sizeof(float) * ((size_t)d.n_groups * p->ldg +
+                                         (size_t)UT_WARPS * d.n_groups * UT_ROWS);
+    if (smem > 48 * 1024)
+      MOC_CUDA_TRY(cudaFuncSetAttribute(update_tiled_kernel,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    update_tiled_kernel<<<RBLOCKS, RTHREADS, smem, p->stream>>>(
+        reinterpret_cast<const float *>(phi), reinterpret_cast<float *>(q), p->xs_order,
+        p->upd_items, p->n_upd_items, p->xs, p->scatter_t, d.fai, d.n_groups, p->ldg,
+        p->scalars, p->partials);
+    update_finalize<<<1, 32, 0, p->stream>>>(p->partials, p->scalars, 1, with_keff ? 1 : 0);
+    MOC_CUDA_TRY(cudaGetLastError());
+    p->launches += 2;
+    return MOC_OK;
+  }
   size_t smem = sizeof(T) * (size_t)p->ldg * (RTHREADS / 32);
   if (with_keff)
     update_kernel<T, true><<<RBLOCKS, RTHREADS, smem, p->stream>>>(
@@ -296,6 +498,29 @@ int keff_t(moc_problem *p, const T *phi) {
 }  // namespace
 
 int moc_post_scratch_blocks() { return RBLOCKS; }
+
+int moc_psi_materialize(moc_problem *p) {
+  if (!p->psi_pending) return MOC_OK;
+  int sms = 0;
+  MOC_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p->device));
+  psi_materialize<<<(unsigned)(sms * 8), RTHREADS, 0, p->stream>>>(p->psi_f, p->n3d * p->ldg,
+                                                                   p->psi_scale);
+  MOC_CUDA_TRY(cudaGetLastError());
+  p->launches++;
+  p->psi_pending = false;
+  return MOC_OK;
+}
+
+int moc_detect_psi_b(moc_problem *p) {
+  MOC_CUDA_TRY(cudaMemsetAsync(p->psi_b_nonzero, 0, sizeof(int32_t), p->stream));
+  int sms = 0;
+  MOC_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p->device));
+  detect_nonzero<<<(unsigned)(sms * 8), RTHREADS, 0, p->stream>>>(p->psi_b, p->n3d * p->ldg,
+                                                                  p->psi_b_nonzero);
+  MOC_CUDA_TRY(cudaGetLastError());
+  p->launches++;
+  return MOC_OK;
+}
 
 int moc_launch_renormalize(moc_problem *p) {
   if (p->mode == MOC_MODE_FP64)

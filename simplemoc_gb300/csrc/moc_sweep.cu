@@ -23,6 +23,11 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <map>
+#include <mutex>
+#include <tuple>
+#include <utility>
+
 #include "moc_internal.h"
 
 namespace {
@@ -43,7 +48,7 @@ __device__ __forceinline__ float div_cr(float a, float b, float rb) {
 
 __device__ __forceinline__ float4 ld_stream(const float *p) {
   float4 v;
-  asm volatile("ld.global.nc.L1::no_allocate.v4.f32 {%0,%1,%2,%3}, [%4];"
+  asm("ld.global.nc.L1::no_allocate.v4.f32 {%0,%1,%2,%3}, [%4];"
                : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
                : "l"(p));
   return v;
@@ -51,8 +56,7 @@ __device__ __forceinline__ float4 ld_stream(const float *p) {
 
 __device__ __forceinline__ void red_add_v4(float *p, float a, float b, float c, float d) {
   asm volatile("red.global.add.v4.f32 [%0], {%1,%2,%3,%4};" ::"l"(p), "f"(a), "f"(b),
-               "f"(c), "f"(d)
-               : "memory");
+               "f"(c), "f"(d));
 }
 
 __device__ __forceinline__ float get(const float4 &v, int e) {
@@ -101,7 +105,8 @@ __device__ __forceinline__ Seg segment_geometry(const SweepArgs &a, float z, int
   // src/solver.c:38-45 (z / dz once: both uses are the same expression)
   int zi = __float2int_rz(div_cr(z, a.dz, a.rdz));
   float zin = __fsub_rn(z, __fmul_rn(a.dz, __fadd_rn(__int2float_rn(zi), 0.5f)));
-  int fine = zi % a.F;
+  // zi % F by a multiply-high; the host verified the magic over every reachable zi
+  int fine = a.fmagic ? zi - a.F * (int)__umulhi((unsigned)zi, a.fmagic) : zi % a.F;
   int r0 = fine;
   if (a.axial_exp == 2) {
     if (fine == 0) {                     // src/solver.c:55-58
@@ -215,6 +220,38 @@ __device__ __forceinline__ void comp_add(float *hi, float *lo, float x) {
   if (err != 0.0f) atomicAdd(lo, err);
 }
 
+// Loads of one segment that are issued one segment ahead (software pipeline):
+// the three fine-source rows (one row for the flat source) of every chunk.
+template <int CPL, bool QUAD>
+struct Rows {
+  float4 v[CPL][QUAD ? 3 : 1];
+};
+
+template <int TPW, int CPL, bool QUAD>
+__device__ __forceinline__ void load_rows(const SweepArgs &a, const Seg &g, int li,
+                                          Rows<CPL, QUAD> &r) {
+#pragma unroll
+  for (int k = 0; k < CPL; ++k) {
+    const int c = li + TPW * k;
+    if (c < a.nchunk) {
+      const float *qr = a.q + g.qrow + 4 * c;
+      r.v[k][0] = ld_stream(qr);
+      if (QUAD) {
+        r.v[k][QUAD ? 1 : 0] = ld_stream(qr + a.ldg);
+        r.v[k][QUAD ? 2 : 0] = ld_stream(qr + 2 * a.ldg);
+      }
+    }
+  }
+}
+
+__device__ __forceinline__ int checked_source(const SweepArgs &a, int s, int li) {
+  if ((uint32_t)s >= (uint64_t)a.ns) {   // validated at upload; never trusted blindly
+    if (li == 0) atomicOr(a.err, 1);
+    return 0;
+  }
+  return s;
+}
+
 template <int TPW, int CPL, int MODE, bool QUAD>
 __global__ void __launch_bounds__(BLOCK) sweep_kernel(SweepArgs a) {
   extern __shared__ float2 s_table[];
@@ -229,6 +266,7 @@ __global__ void __launch_bounds__(BLOCK) sweep_kernel(SweepArgs a) {
   const int64_t warp_id = ((int64_t)blockIdx.x * BLOCK + threadIdx.x) >> 5;
   const int64_t n_warps = ((int64_t)gridDim.x * BLOCK) >> 5;
   const int64_t PZ = (int64_t)a.P * a.Z;
+  const int S = a.S;
 
   for (int64_t base = warp_id * GPW; base < a.n3d; base += n_warps * GPW) {
     const int64_t track = base + gw;
@@ -241,8 +279,8 @@ __global__ void __launch_bounds__(BLOCK) sweep_kernel(SweepArgs a) {
     const float w = a.weight[tr];
     const float w_mu = __fmul_rn(w, mu);
     float z = a.z0[tr];
-    const float *dsb = a.seg_ds + (i2 * a.P + j) * a.S;
-    const int32_t *srcb = a.seg_src + tr * a.S;
+    const float *dsb = a.seg_ds + (i2 * a.P + j) * S;
+    const int32_t *srcb = a.seg_src + tr * S;
 
     float4 psi[CPL];
 #pragma unroll
@@ -250,88 +288,118 @@ __global__ void __launch_bounds__(BLOCK) sweep_kernel(SweepArgs a) {
       const int c = li + TPW * k;
       psi[k] = make_float4(0.f, 0.f, 0.f, 0.f);
       if (c < a.nchunk) psi[k] = *reinterpret_cast<const float4 *>(a.psi + tr * a.ldg + 4 * c);
+      if (a.psi_scale) {                    // renormalisation still to apply (src/solver.c:1224)
+        const float sc = *a.psi_scale;
+        psi[k].x = __fmul_rn(psi[k].x, sc);
+        psi[k].y = __fmul_rn(psi[k].y, sc);
+        psi[k].z = __fmul_rn(psi[k].z, sc);
+        psi[k].w = __fmul_rn(psi[k].w, sc);
+      }
     }
 
-    for (int n0 = 0; n0 < a.S; n0 += TPW) {
-      const int nl = n0 + li;
-      const float my_ds = nl < a.S ? __ldg(dsb + nl) : 0.f;
-      const int my_src = nl < a.S ? __ldg(srcb + nl) : 0;
-      const int cnt = min(TPW, a.S - n0);
-      for (int nn = 0; nn < cnt; ++nn) {
-        const float ds = __shfl_sync(FULL, my_ds, nn, TPW);
-        int s = __shfl_sync(FULL, my_src, nn, TPW);
-        if ((uint32_t)s >= (uint64_t)a.ns) {   // checked at upload; never trusted blindly
-          if (li == 0) atomicOr(a.err, 1);
-          s = 0;
+    // segment streams: the current chunk of TPW entries and the next one
+    float ds_c = li < S ? __ldg(dsb + li) : 0.f;
+    int src_c = li < S ? __ldg(srcb + li) : 0;
+    float ds_n = TPW + li < S ? __ldg(dsb + TPW + li) : 0.f;
+    int src_n = TPW + li < S ? __ldg(srcb + TPW + li) : 0;
+
+    float ds = __shfl_sync(FULL, ds_c, 0, TPW);
+    Seg g = segment_geometry(a, z, checked_source(a, __shfl_sync(FULL, src_c, 0, TPW), li));
+    Rows<CPL, QUAD> rows;
+    load_rows<TPW, CPL, QUAD>(a, g, li, rows);
+
+    for (int n = 0; n < S; ++n) {
+      const float z_next = advance_z(a, z, ds, mu);
+      // ---- issue the loads of segment n+1 before the arithmetic of segment n
+      float ds1 = 0.f;
+      Seg g1 = g;
+      Rows<CPL, QUAD> rows1 = rows;
+      const int m = n + 1;
+      if (m < S) {
+        const int k = m & (TPW - 1);
+        if (k == 0) {
+          ds_c = ds_n;
+          src_c = src_n;
+          const int nl = m + TPW + li;
+          ds_n = nl < S ? __ldg(dsb + nl) : 0.f;
+          src_n = nl < S ? __ldg(srcb + nl) : 0;
         }
-        const Seg g = segment_geometry(a, z, s);
+        ds1 = __shfl_sync(FULL, ds_c, k, TPW);
+        g1 = segment_geometry(a, z_next, checked_source(a, __shfl_sync(FULL, src_c, k, TPW), li));
+        load_rows<TPW, CPL, QUAD>(a, g1, li, rows1);
+      }
+      // ---- segment n
 #pragma unroll
-        for (int k = 0; k < CPL; ++k) {
-          const int c = li + TPW * k;
-          if (c >= a.nchunk) continue;
-          const int g4 = 4 * c;
-          const float *cf = a.coef + g.crow + g4;
-          const float4 sig = __ldg(reinterpret_cast<const float4 *>(cf));
-          const float4 r1 = __ldg(reinterpret_cast<const float4 *>(cf + 4 * a.ldg));
-          float4 t;
-          if (QUAD) {
-            const float *qr = a.q + g.qrow + g4;
-            const float4 y1 = ld_stream(qr);
-            const float4 y2 = ld_stream(qr + a.ldg);
-            const float4 y3 = ld_stream(qr + 2 * a.ldg);
+      for (int k = 0; k < CPL; ++k) {
+        const int c = li + TPW * k;
+        if (c >= a.nchunk) continue;
+        const int g4 = 4 * c;
+        const float *cf = a.coef + g.crow + g4;
+        const float4 sig = __ldg(reinterpret_cast<const float4 *>(cf));
+        const float4 r1 = __ldg(reinterpret_cast<const float4 *>(cf + 4 * a.ldg));
+        float4 t;
+        if (QUAD) {
+          const float4 y1 = rows.v[k][0];
+          const float4 y2 = rows.v[k][QUAD ? 1 : 0];
+          const float4 y3 = rows.v[k][QUAD ? 2 : 0];
+          if (MODE == MODE_PLAIN) {
             const float4 r2 = __ldg(reinterpret_cast<const float4 *>(cf + 5 * a.ldg));
             const float4 r3 = __ldg(reinterpret_cast<const float4 *>(cf + 6 * a.ldg));
             const float4 r4 = __ldg(reinterpret_cast<const float4 *>(cf + 7 * a.ldg));
-            if (MODE == MODE_PLAIN) {
-              const float4 sig2 = __ldg(reinterpret_cast<const float4 *>(cf + 1 * a.ldg));
-              const float4 sig3 = __ldg(reinterpret_cast<const float4 *>(cf + 2 * a.ldg));
-              const float4 sig4 = __ldg(reinterpret_cast<const float4 *>(cf + 3 * a.ldg));
-#pragma unroll
-              for (int e = 0; e < 4; ++e) {
-                float p = get(psi[k], e);
-                set(t, e, plain_quad(a, s_table, get(y1, e), get(y2, e), get(y3, e), get(sig, e),
-                                     get(sig2, e), get(sig3, e), get(sig4, e), get(r1, e),
-                                     get(r2, e), get(r3, e), get(r4, e), g.zin, ds, mu, mu2, w,
-                                     p));
-                set(psi[k], e, p);
-              }
-            } else {
-#pragma unroll
-              for (int e = 0; e < 4; ++e) {
-                float p = get(psi[k], e);
-                set(t, e, mixed_quad(a, get(y1, e), get(y2, e), get(y3, e), get(sig, e),
-                                     get(r1, e), get(r2, e), get(r3, e), get(r4, e), g.zin, ds,
-                                     mu, mu2, w, p));
-                set(psi[k], e, p);
-              }
-            }
-          } else {
-            const float4 y = ld_stream(a.q + g.qrow + g4);
 #pragma unroll
             for (int e = 0; e < 4; ++e) {
+              // the reference's divisors, formed with its own operations
+              const float sg = get(sig, e);
+              const float sg2 = __fmul_rn(sg, sg);                        // solver.c:153
+              const float sg3 = __fmul_rn(sg, sg2);                       // solver.c:176
+              const float sg4 = __fmul_rn(__fmul_rn(3.f, sg2), sg2);      // solver.c:198
               float p = get(psi[k], e);
-              if (MODE == MODE_PLAIN)
-                set(t, e, plain_flat(a, s_table, get(y, e), get(sig, e), get(r1, e), ds, w_mu, p));
-              else
-                set(t, e, mixed_flat(get(y, e), get(sig, e), get(r1, e), ds, w_mu, p));
+              set(t, e, plain_quad(a, s_table, get(y1, e), get(y2, e), get(y3, e), sg, sg2, sg3,
+                                   sg4, get(r1, e), get(r2, e), get(r3, e), get(r4, e), g.zin,
+                                   ds, mu, mu2, w, p));
+              set(psi[k], e, p);
+            }
+          } else {
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+              const float q1r = get(r1, e);
+              const float q2r = q1r * q1r;
+              float p = get(psi[k], e);
+              set(t, e, mixed_quad(a, get(y1, e), get(y2, e), get(y3, e), get(sig, e), q1r, q2r,
+                                   q1r * q2r, q2r * q2r * (1.0f / 3.0f), g.zin, ds, mu, mu2, w,
+                                   p));
               set(psi[k], e, p);
             }
           }
-          if (valid) {
-            float *dst = a.phi + g.frow + g4;
-            if (MODE == MODE_MIXED && a.phi_lo != nullptr) {
-              float *lo = a.phi_lo + g.frow + g4;
-              comp_add(dst + 0, lo + 0, t.x);
-              comp_add(dst + 1, lo + 1, t.y);
-              comp_add(dst + 2, lo + 2, t.z);
-              comp_add(dst + 3, lo + 3, t.w);
-            } else {
-              red_add_v4(dst, t.x, t.y, t.z, t.w);
-            }
+        } else {
+          const float4 y = rows.v[k][0];
+#pragma unroll
+          for (int e = 0; e < 4; ++e) {
+            float p = get(psi[k], e);
+            if (MODE == MODE_PLAIN)
+              set(t, e, plain_flat(a, s_table, get(y, e), get(sig, e), get(r1, e), ds, w_mu, p));
+            else
+              set(t, e, mixed_flat(get(y, e), get(sig, e), get(r1, e), ds, w_mu, p));
+            set(psi[k], e, p);
           }
         }
-        z = advance_z(a, z, ds, mu);
+        if (valid) {
+          float *dst = a.phi + g.frow + g4;
+          if (MODE == MODE_MIXED && a.phi_lo != nullptr) {
+            float *lo = a.phi_lo + g.frow + g4;
+            comp_add(dst + 0, lo + 0, t.x);
+            comp_add(dst + 1, lo + 1, t.y);
+            comp_add(dst + 2, lo + 2, t.z);
+            comp_add(dst + 3, lo + 3, t.w);
+          } else {
+            red_add_v4(dst, t.x, t.y, t.z, t.w);
+          }
+        }
       }
+      z = z_next;
+      ds = ds1;
+      g = g1;
+      rows = rows1;
     }
     if (valid) {
 #pragma unroll
@@ -477,39 +545,29 @@ int dispatch_shape(moc_problem *p, const SweepArgs &a, int tpw, int cpl) {
 
 }  // namespace
 
-// Chooses the threads-per-track and chunks-per-thread for a group count: the
-// smallest shape whose TPW*CPL chunks cover the ldg/4 chunks, preferring more
-// threads per track (more tracks in flight per SM is what hides gather latency).
+// Default threads-per-track and chunks-per-thread for a group count, from the
+// launch-shape measurements on GB300 (two tracks per warp with two chunks per
+// thread was fastest for 100 groups in both modes); moc_autotune measures.
 int moc_sweep_launch_shape(const moc_problem *p, int *tpw, int *cpl) {
-  int nchunk = p->ldg / 4;
+  const int nchunk = p->ldg / 4;
   if (p->tpw > 0) {
     *tpw = p->tpw;
     *cpl = p->cpl;
     if ((int64_t)p->tpw * p->cpl < nchunk) return MOC_ERR_ARG;
     return MOC_OK;
   }
-  static const int shapes[][2] = {{4, 2}, {8, 1}, {16, 1}, {8, 4}, {32, 1}, {16, 2},
-                                  {32, 2}, {32, 4}};
-  // prefer the shape with the best lane utilisation, then the fewest chunks per thread
-  int best = -1;
-  double best_util = -1.0;
-  for (int i = 0; i < 8; ++i) {
-    int cap = shapes[i][0] * shapes[i][1];
-    if (cap < nchunk) continue;
-    double util = (double)nchunk / cap;
-    if (util > best_util + 1e-9 ||
-        (util > best_util - 1e-9 && best >= 0 && shapes[i][1] < shapes[best][1])) {
-      best = i;
-      best_util = util;
-    }
-  }
-  if (best < 0) return MOC_ERR_UNSUPPORTED;
-  *tpw = shapes[best][0];
-  *cpl = shapes[best][1];
+  if (nchunk <= 8) { *tpw = 8; *cpl = 1; }
+  else if (nchunk <= 16) { *tpw = 16; *cpl = 1; }
+  else if (nchunk <= 32) { *tpw = 16; *cpl = 2; }
+  else if (nchunk <= 64) { *tpw = 32; *cpl = 2; }
+  else if (nchunk <= 128) { *tpw = 32; *cpl = 4; }
+  else return MOC_ERR_UNSUPPORTED;
   return MOC_OK;
 }
 
-int moc_launch_sweep(moc_problem *p) {
+namespace {
+
+SweepArgs build_args(moc_problem *p) {
   const moc_dims &d = p->d;
   SweepArgs a{};
   a.seg_ds = p->seg_ds;
@@ -524,6 +582,7 @@ int moc_launch_sweep(moc_problem *p) {
   a.phi = p->phi;
   a.phi_lo = (p->mode == MOC_MODE_MIXED && (p->flags & MOC_FLAG_COMPENSATED)) ? p->phi_lo : nullptr;
   a.psi = p->psi_f;
+  a.psi_scale = (p->psi_pending && p->mode != MOC_MODE_FP64) ? p->psi_scale : nullptr;
   a.q64 = p->q64;
   a.phi64 = p->phi64;
   a.psi64 = p->psi_f64;
@@ -550,18 +609,125 @@ int moc_launch_sweep(moc_problem *p) {
   a.d2 = 2.f * a.dz * a.dz;               // src/solver.c:76
   a.rd2 = 1.0f / a.d2;
   a.hd = d.height / (float)d.decomp_ax;
+  a.fmagic = p->fmagic;
   a.err = p->err;
-  const bool quad = d.axial_exp == 2;
+  return a;
+}
+
+int launch_args(moc_problem *p, const SweepArgs &a, int tpw, int cpl) {
+  const bool quad = p->d.axial_exp == 2;
   if (p->mode == MOC_MODE_FP64) {
     if (!p->q64) return MOC_ERR_STATE;
     return quad ? launch64_t<32, true>(p, a) : launch64_t<32, false>(p, a);
   }
-  int tpw = 0, cpl = 0;
-  int st = moc_sweep_launch_shape(p, &tpw, &cpl);
-  if (st != MOC_OK) return st;
   if (p->mode == MOC_MODE_PLAIN)
     return quad ? dispatch_shape<MODE_PLAIN, true>(p, a, tpw, cpl)
                 : dispatch_shape<MODE_PLAIN, false>(p, a, tpw, cpl);
   return quad ? dispatch_shape<MODE_MIXED, true>(p, a, tpw, cpl)
               : dispatch_shape<MODE_MIXED, false>(p, a, tpw, cpl);
+}
+
+struct TuneKey {
+  int S, G, P, mode, axial, comp;
+  bool operator<(const TuneKey &o) const {
+    return std::tie(S, G, P, mode, axial, comp) < std::tie(o.S, o.G, o.P, o.mode, o.axial, o.comp);
+  }
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, std::pair<int, int>> g_tune_cache;
+
+}  // namespace
+
+int moc_launch_sweep(moc_problem *p) {
+  int tpw = 0, cpl = 0;
+  int st = moc_sweep_launch_shape(p, &tpw, &cpl);
+  if (st != MOC_OK) return st;
+  return launch_args(p, build_args(p), tpw, cpl);
+}
+
+// Times every launch shape that covers the groups on the first n_sub tracks.
+// Tallies go to a scratch copy of the flux array and the tracks' angular flux
+// to a scratch copy, so the problem's state is not changed.
+int moc_sweep_autotune(moc_problem *p, int64_t n_sub, int *tpw_out, int *cpl_out,
+                       double *ms_out) {
+  if (p->mode == MOC_MODE_FP64) {
+    *tpw_out = 32;
+    *cpl_out = 1;
+    if (ms_out) *ms_out = 0.0;
+    return MOC_OK;
+  }
+  const TuneKey key{p->d.n_seg, p->d.n_groups, p->d.n_polar, p->mode, p->d.axial_exp,
+                    (p->flags & MOC_FLAG_COMPENSATED) ? 1 : 0};
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    auto it = g_tune_cache.find(key);
+    if (it != g_tune_cache.end() && ms_out == nullptr) {
+      *tpw_out = it->second.first;
+      *cpl_out = it->second.second;
+      return MOC_OK;
+    }
+  }
+  if (n_sub <= 0) n_sub = p->n3d < 262144 ? p->n3d : 262144;
+  if (n_sub > p->n3d) n_sub = p->n3d;
+  float *phi_s = nullptr, *psi_s = nullptr, *lo_s = nullptr;
+  const size_t phi_bytes = sizeof(float) * (size_t)(p->nfsr * p->ldg);
+  const size_t psi_bytes = sizeof(float) * (size_t)(n_sub * p->ldg);
+  MOC_CUDA_TRY(cudaMalloc(&phi_s, phi_bytes));
+  if (cudaMalloc(&psi_s, psi_bytes) != cudaSuccess ||
+      (p->phi_lo && cudaMalloc(&lo_s, phi_bytes) != cudaSuccess)) {
+    cudaGetLastError();
+    cudaFree(phi_s);
+    cudaFree(psi_s);
+    return MOC_ERR_OOM;
+  }
+  SweepArgs a = build_args(p);
+  a.n3d = n_sub;
+  a.phi = phi_s;
+  a.psi = psi_s;
+  if (a.phi_lo) a.phi_lo = lo_s;
+  int rc = MOC_OK;
+  if (cudaMemsetAsync(phi_s, 0, phi_bytes, p->stream) != cudaSuccess ||
+      (lo_s && cudaMemsetAsync(lo_s, 0, phi_bytes, p->stream) != cudaSuccess) ||
+      cudaMemcpyAsync(psi_s, p->psi_f, psi_bytes, cudaMemcpyDeviceToDevice, p->stream) !=
+          cudaSuccess)
+    rc = MOC_ERR_CUDA;
+  static const int shapes[][2] = {{32, 1}, {32, 2}, {32, 4}, {16, 1}, {16, 2}, {8, 1}, {8, 4}, {4, 2}};
+  const int nchunk = p->ldg / 4;
+  double best = 1e30;
+  int bt = 0, bc = 0;
+  for (auto &sh : shapes) {
+    if (rc != MOC_OK) break;
+    if ((int64_t)sh[0] * sh[1] < nchunk) continue;
+    if ((int64_t)sh[0] * sh[1] >= 4 * (int64_t)nchunk && sh[1] > 1) continue;   // mostly idle lanes
+    rc = launch_args(p, a, sh[0], sh[1]);                    // warm-up
+    double tot = 0.0;
+    for (int r = 0; r < 2 && rc == MOC_OK; ++r) {
+      cudaEventRecord(p->ev0, p->stream);
+      rc = launch_args(p, a, sh[0], sh[1]);
+      cudaEventRecord(p->ev1, p->stream);
+      if (rc == MOC_OK && cudaEventSynchronize(p->ev1) != cudaSuccess) rc = MOC_ERR_CUDA;
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, p->ev0, p->ev1);
+      tot += ms;
+    }
+    if (rc == MOC_OK && tot / 2 < best) {
+      best = tot / 2;
+      bt = sh[0];
+      bc = sh[1];
+    }
+  }
+  cudaStreamSynchronize(p->stream);
+  cudaFree(phi_s);
+  cudaFree(psi_s);
+  if (lo_s) cudaFree(lo_s);
+  if (rc != MOC_OK) return rc;
+  if (bt == 0) return MOC_ERR_UNSUPPORTED;
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    g_tune_cache[key] = {bt, bc};
+  }
+  *tpw_out = bt;
+  *cpl_out = bc;
+  if (ms_out) *ms_out = best;
+  return MOC_OK;
 }

@@ -74,6 +74,13 @@ class Solver:
         L.check(self._lib.moc_get_launch(self._h, C.byref(a), C.byref(b)), "moc_get_launch")
         return a.value, b.value
 
+    def autotune(self, n_tracks: int = 0, measure: bool = True) -> tuple[int, int, float]:
+        """Picks the fastest launch shape for the current mode (moc_autotune)."""
+        a, b, ms = C.c_int(), C.c_int(), C.c_double()
+        L.check(self._lib.moc_autotune(self._h, n_tracks, C.byref(a), C.byref(b),
+                                       C.byref(ms) if measure else None), "moc_autotune")
+        return a.value, b.value, ms.value
+
     def upload(self, problem: HostProblem | None = None) -> None:
         p = problem or self.problem
         self._host = p.host()
