@@ -43,6 +43,20 @@ class OracleProblem(C.Structure):
     ]
 
 
+class OracleRefGeo(C.Structure):
+    _fields_ = [("N2D", C.c_int64), ("seg_off", i64p), ("seg_len", f32p), ("az_weight", f32p),
+                ("p_weight", f32p), ("axial_z_sep", C.c_float)]
+
+
+def make_refgeo(geo) -> OracleRefGeo:
+    """oracle_refgeo over a simplemoc_gb300.refabi.RefGeometry (duck-typed)."""
+    g = OracleRefGeo(N2D=len(geo.seg_off) - 1, seg_off=_p(geo.seg_off, C.c_int64),
+                     seg_len=_p(geo.seg_len, C.c_float), az_weight=_p(geo.az_weight, C.c_float),
+                     p_weight=_p(geo.p_weight, C.c_float), axial_z_sep=geo.axial_z_sep)
+    g._keep = geo
+    return g
+
+
 def build(reference: bool | None = None) -> None:
     """make -C oracle port [ref]; `ref` only where the reference sources exist."""
     targets = ["port"]
@@ -102,6 +116,8 @@ class Port:
             "oracle_renormalize64": (None, [P, f64p, f64p, f64p]),
             "oracle_update_sources64": (C.c_double, [P, f64p, f64p, C.c_double]),
             "oracle_compute_keff64": (C.c_double, [P, f64p, C.c_double]),
+            "oracle_ref_sweep": (C.c_int64, [P, C.POINTER(OracleRefGeo), f32p, f32p, f32p, f32p,
+                                             i32p]),
         }
         for n, (r, a) in sig.items():
             fn = getattr(lib, n)
@@ -134,6 +150,12 @@ class Port:
         self.lib.oracle_sweep_tracks(C.byref(op), _p(q, f), _p(tracks, C.c_int64), len(tracks),
                                      _p(psi_in, f), _p(out, f), _p(phi, f))
         return out
+
+    def ref_sweep(self, op, rg, q, phi, psi_f, z_height, ids=None) -> int:
+        """The reference traversal (oracle_ref_sweep); ids None = libc rand()."""
+        f = C.c_float
+        return self.lib.oracle_ref_sweep(C.byref(op), C.byref(rg), _p(q, f), _p(phi, f),
+                                         _p(psi_f, f), _p(z_height, f), _p(ids, C.c_int32))
 
     def renormalize(self, op, phi, psi_f, psi_b) -> None:
         f = C.c_float
@@ -223,6 +245,23 @@ class Reference:
         dx, mv = C.c_float(), C.c_float()
         n = self.lib.refh_table(precision, _p(vals, C.c_float), cap, C.byref(dx), C.byref(mv))
         return vals[:2 * n].copy(), dx.value, mv.value, n
+
+    def transport_sweep(self, hp, state: dict, rg, z_height) -> int:
+        """The reference's own transport_sweep (serial build: libc rand() ids,
+        seeded by the caller's srand) over a reference-style geometry."""
+        op = make_problem(hp)
+        f = C.c_float
+        self.lib.refh_setup_ref.argtypes = [C.POINTER(OracleRefGeo), f32p, C.c_float]
+        self.lib.refh_transport_sweep.restype = C.c_long
+        self.lib.refh_transport_sweep.argtypes = [f32p]
+        self.lib.refh_setup(C.byref(op), hp.spec.precision, _p(state["fine_source"], f),
+                            _p(state["fine_flux"], f), _p(state["psi_f"], f),
+                            _p(state["psi_b"], f))
+        try:
+            self.lib.refh_setup_ref(C.byref(rg), _p(z_height, f), rg.axial_z_sep)
+            return int(self.lib.refh_transport_sweep(_p(z_height, f)))
+        finally:
+            self.lib.refh_teardown()
 
     def iterate(self, hp, state: dict, n_iters: int, keff: float = 1.0, sweep_only=False):
         op = make_problem(hp)

@@ -24,7 +24,7 @@ BUILD = PKG / "_build"
 LIB = PKG / "libsimplemoc_gb300.so"
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
-CU_SOURCES = ["moc_api.cu", "moc_sweep.cu", "moc_post.cu"]
+CU_SOURCES = ["moc_api.cu", "moc_sweep.cu", "moc_post.cu", "moc_refabi.cu"]
 CPP_SOURCES = ["moc_host.cpp"]
 
 
@@ -73,8 +73,10 @@ def build(verbose: bool = False) -> Path:
         list(ex.map(_run, jobs))
     if jobs or _stale(LIB, objs):
         tmp = LIB.with_suffix(".so.tmp")
+        # -Bsymbolic: calls inside the library bind to its own definitions even when
+        # another loaded object exports the same reference entry-point names
         _run([_nvcc(), ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-Xcompiler", "-fopenmp",
-              "-lgomp"])
+              "-Xlinker", "-Bsymbolic", "-lgomp"])
         os.replace(tmp, LIB)
     return LIB
 

@@ -43,6 +43,11 @@ struct SweepArgs {
   float hd;                 // domain height
   uint32_t fmagic;          // zi % F == zi - F*umulhi(zi, fmagic) for reachable zi; 0 = use %
   int32_t *err;             // device error word (0 = ok)
+  // variable-length sub-segment streams (reference traversal), else null
+  const int64_t *csr_off;   // [N3D+1]
+  const float *csr_ds;      // [M] sub-segment lengths
+  const float *csr_z;       // [M] start heights
+  const int32_t *csr_src;   // [M] source regions
 };
 
 struct moc_problem {
@@ -91,6 +96,8 @@ struct moc_problem {
 
 // Launchers implemented in moc_sweep.cu / moc_post.cu.
 int moc_launch_sweep(moc_problem *p);
+int moc_launch_sweep_csr(moc_problem *p, const int64_t *off, const float *ds, const float *z,
+                         const int32_t *src);
 int moc_sweep_launch_shape(const moc_problem *p, int *tpw, int *cpl);
 int moc_sweep_autotune(moc_problem *p, int64_t n_sub, int *tpw, int *cpl, double *ms);
 int moc_launch_renormalize(moc_problem *p);

@@ -252,7 +252,11 @@ __device__ __forceinline__ int checked_source(const SweepArgs &a, int s, int li)
   return s;
 }
 
-template <int TPW, int CPL, int MODE, bool QUAD>
+// CSR: the tracks' segment streams are variable-length (the reference
+// traversal's sub-segments, csr_off/csr_ds/csr_z/csr_src) with the start height
+// of every sub-segment given; otherwise every track has S segments and its
+// height advances by ds*mu.  CSR runs one track per warp (TPW == 32).
+template <int TPW, int CPL, int MODE, bool QUAD, bool CSR = false>
 __global__ void __launch_bounds__(BLOCK) sweep_kernel(SweepArgs a) {
   extern __shared__ float2 s_table[];
   if (MODE == MODE_PLAIN) {
@@ -266,7 +270,7 @@ __global__ void __launch_bounds__(BLOCK) sweep_kernel(SweepArgs a) {
   const int64_t warp_id = ((int64_t)blockIdx.x * BLOCK + threadIdx.x) >> 5;
   const int64_t n_warps = ((int64_t)gridDim.x * BLOCK) >> 5;
   const int64_t PZ = (int64_t)a.P * a.Z;
-  const int S = a.S;
+  static_assert(!CSR || TPW == 32, "variable-length streams run one track per warp");
 
   for (int64_t base = warp_id * GPW; base < a.n3d; base += n_warps * GPW) {
     const int64_t track = base + gw;
@@ -278,9 +282,24 @@ __global__ void __launch_bounds__(BLOCK) sweep_kernel(SweepArgs a) {
     const float mu2 = __fmul_rn(mu, mu);
     const float w = a.weight[tr];
     const float w_mu = __fmul_rn(w, mu);
-    float z = a.z0[tr];
-    const float *dsb = a.seg_ds + (i2 * a.P + j) * S;
-    const int32_t *srcb = a.seg_src + tr * S;
+    float z;
+    int S;
+    const float *dsb;
+    const int32_t *srcb;
+    const float *zb = nullptr;
+    if (CSR) {
+      const int64_t o0 = a.csr_off[tr];
+      S = (int)(a.csr_off[tr + 1] - o0);
+      dsb = a.csr_ds + o0;
+      srcb = a.csr_src + o0;
+      zb = a.csr_z + o0;
+      z = 0.f;
+    } else {
+      S = a.S;
+      z = a.z0[tr];
+      dsb = a.seg_ds + (i2 * a.P + j) * S;
+      srcb = a.seg_src + tr * S;
+    }
 
     float4 psi[CPL];
 #pragma unroll
@@ -302,14 +321,20 @@ __global__ void __launch_bounds__(BLOCK) sweep_kernel(SweepArgs a) {
     int src_c = li < S ? __ldg(srcb + li) : 0;
     float ds_n = TPW + li < S ? __ldg(dsb + TPW + li) : 0.f;
     int src_n = TPW + li < S ? __ldg(srcb + TPW + li) : 0;
+    float z_c = 0.f, z_n = 0.f;
+    if (CSR) {
+      z_c = li < S ? __ldg(zb + li) : 0.f;
+      z_n = TPW + li < S ? __ldg(zb + TPW + li) : 0.f;
+      z = __shfl_sync(FULL, z_c, 0, TPW);
+    }
 
     float ds = __shfl_sync(FULL, ds_c, 0, TPW);
     Seg g = segment_geometry(a, z, checked_source(a, __shfl_sync(FULL, src_c, 0, TPW), li));
     Rows<CPL, QUAD> rows;
-    load_rows<TPW, CPL, QUAD>(a, g, li, rows);
+    if (S > 0) load_rows<TPW, CPL, QUAD>(a, g, li, rows);
 
     for (int n = 0; n < S; ++n) {
-      const float z_next = advance_z(a, z, ds, mu);
+      float z_next = CSR ? 0.f : advance_z(a, z, ds, mu);
       // ---- issue the loads of segment n+1 before the arithmetic of segment n
       float ds1 = 0.f;
       Seg g1 = g;
@@ -323,7 +348,12 @@ __global__ void __launch_bounds__(BLOCK) sweep_kernel(SweepArgs a) {
           const int nl = m + TPW + li;
           ds_n = nl < S ? __ldg(dsb + nl) : 0.f;
           src_n = nl < S ? __ldg(srcb + nl) : 0;
+          if (CSR) {
+            z_c = z_n;
+            z_n = nl < S ? __ldg(zb + nl) : 0.f;
+          }
         }
+        if (CSR) z_next = __shfl_sync(FULL, z_c, k, TPW);
         ds1 = __shfl_sync(FULL, ds_c, k, TPW);
         g1 = segment_geometry(a, z_next, checked_source(a, __shfl_sync(FULL, src_c, k, TPW), li));
         load_rows<TPW, CPL, QUAD>(a, g1, li, rows1);
@@ -489,9 +519,9 @@ __global__ void __launch_bounds__(BLOCK) sweep64_kernel(SweepArgs a) {
   }
 }
 
-template <int TPW, int CPL, int MODE, bool QUAD>
+template <int TPW, int CPL, int MODE, bool QUAD, bool CSR = false>
 int launch_t(moc_problem *p, const SweepArgs &a) {
-  auto kern = sweep_kernel<TPW, CPL, MODE, QUAD>;
+  auto kern = sweep_kernel<TPW, CPL, MODE, QUAD, CSR>;
   size_t smem = (MODE == MODE_PLAIN) ? sizeof(float2) * (size_t)a.table_n : 0;
   if (smem > 48 * 1024) {
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
@@ -730,4 +760,34 @@ int moc_sweep_autotune(moc_problem *p, int64_t n_sub, int *tpw_out, int *cpl_out
   *cpl_out = bc;
   if (ms_out) *ms_out = best;
   return MOC_OK;
+}
+
+// Sweep over variable-length sub-segment streams (the reference traversal).
+int moc_launch_sweep_csr(moc_problem *p, const int64_t *off, const float *ds, const float *z,
+                         const int32_t *src) {
+  SweepArgs a = build_args(p);
+  a.csr_off = off;
+  a.csr_ds = ds;
+  a.csr_z = z;
+  a.csr_src = src;
+  const bool quad = p->d.axial_exp == 2;
+  const int nchunk = p->ldg / 4;
+  if (p->mode == MOC_MODE_FP64) return MOC_ERR_UNSUPPORTED;
+  const bool plain = p->mode == MOC_MODE_PLAIN;
+  if (nchunk <= 32)
+    return plain ? (quad ? launch_t<32, 1, MODE_PLAIN, true, true>(p, a)
+                         : launch_t<32, 1, MODE_PLAIN, false, true>(p, a))
+                 : (quad ? launch_t<32, 1, MODE_MIXED, true, true>(p, a)
+                         : launch_t<32, 1, MODE_MIXED, false, true>(p, a));
+  if (nchunk <= 64)
+    return plain ? (quad ? launch_t<32, 2, MODE_PLAIN, true, true>(p, a)
+                         : launch_t<32, 2, MODE_PLAIN, false, true>(p, a))
+                 : (quad ? launch_t<32, 2, MODE_MIXED, true, true>(p, a)
+                         : launch_t<32, 2, MODE_MIXED, false, true>(p, a));
+  if (nchunk <= 128)
+    return plain ? (quad ? launch_t<32, 4, MODE_PLAIN, true, true>(p, a)
+                         : launch_t<32, 4, MODE_PLAIN, false, true>(p, a))
+                 : (quad ? launch_t<32, 4, MODE_MIXED, true, true>(p, a)
+                         : launch_t<32, 4, MODE_MIXED, false, true>(p, a));
+  return MOC_ERR_UNSUPPORTED;
 }

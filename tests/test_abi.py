@@ -19,6 +19,12 @@ def declared_functions():
     return sorted(set(n for n in names if not n.startswith("_")))
 
 
+def declared_functions_in(header: str):
+    text = re.sub(r"/\*.*?\*/", "", (ROOT / "include" / header).read_text(), flags=re.S)
+    return re.findall(r"^\s*(?:const\s+)?[A-Za-z_][A-Za-z0-9_]*\s*\**\s*"
+                      r"([A-Za-z_][A-Za-z0-9_]*)\s*\(", text, flags=re.M)
+
+
 def test_library_exports_every_declared_symbol(lib):
     names = declared_functions()
     assert len(names) >= 20
@@ -26,11 +32,20 @@ def test_library_exports_every_declared_symbol(lib):
     assert not missing, missing
 
 
-def test_binding_covers_every_declared_symbol():
+def test_binding_covers_every_declared_symbol(lib):
     from simplemoc_gb300 import _lib as L
-    # the reference-signature shims are bound by their own module
-    names = [n for n in declared_functions() if n.startswith("moc_")]
-    missing = [n for n in names if n not in L.SIGNATURES]
+    from simplemoc_gb300 import refabi
+    refabi.lib()
+    # the flat ABI is bound in _lib.SIGNATURES, the reference-signature entry
+    # points (include/simplemoc_refabi.h) by simplemoc_gb300.refabi
+    ref_names = set(declared_functions_in("simplemoc_refabi.h"))
+    missing = []
+    for n in declared_functions():
+        if n in ref_names:
+            if getattr(lib, n).argtypes is None:
+                missing.append(n)
+        elif n not in L.SIGNATURES:
+            missing.append(n)
     assert not missing, missing
 
 
