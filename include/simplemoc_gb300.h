@@ -201,6 +201,34 @@ int moc_time_power_iterations(moc_problem *p, int iters, double *ms_total,
 /* Number of kernels the library has launched on this handle so far. */
 int64_t moc_launch_count(const moc_problem *p);
 
+/* ---- batched sweep of independent problems ------------------------------ */
+/* Many independent problems ("cores", e.g. small reactor cores of different
+ * sizes and group counts) on one device, swept by ONE persistent launch: warps
+ * take (core, tracks) tasks from a work counter, the largest first, each core
+ * with its own threads per track.  The batch references the problems (they
+ * stay owned by the caller and keep their own state); all must share the
+ * device, mode (PLAIN or MIXED), source order and exponential table, and have
+ * at most 128 groups. */
+typedef struct moc_batch moc_batch;
+int moc_batch_create(int n, moc_problem *const *problems, moc_batch **out);
+int moc_batch_destroy(moc_batch *b);
+/* Autotuner of the batch: per distinct (segments per track, groups, polar
+ * angles, mode) the threads per track of the fastest measured launch. */
+int moc_batch_autotune(moc_batch *b);
+int moc_batch_set_width(moc_batch *b, int core, int threads_per_track);
+int moc_batch_widths(const moc_batch *b, int *threads_per_track);
+/* One batched transport sweep (waits for it). */
+int moc_batch_sweep(moc_batch *b);
+/* `iters` power iterations of every core (batched sweep, then each core's
+ * renormalize_flux / update_sources / compute_keff with k_eff kept on the
+ * device); use_graph captures one iteration as a CUDA graph and replays it.
+ * *ms_total = device time of the iterations (events on the batch stream). */
+int moc_batch_power_iterations(moc_batch *b, int iters, int use_graph,
+                               double *ms_total);
+/* Per-core k_eff and source residual of the last iteration. */
+int moc_batch_results(moc_batch *b, double *keff, double *residual);
+int64_t moc_batch_launch_count(const moc_batch *b);
+
 /* ---- renormalize_flux without device allocation ------------------------ */
 /* No counterpart in the reference.  For callers that cannot let the library
  * call cudaMalloc (a framework or pool allocator that accounts for every

@@ -99,6 +99,15 @@ SIGNATURES = {
     "moc_time_sweep": (C.c_int, [C.c_void_p, C.c_int, f64p]),
     "moc_launch_count": (C.c_int64, [C.c_void_p]),
     "moc_time_power_iterations": (C.c_int, [C.c_void_p, C.c_int, f64p, f64p, f64p, f64p]),
+    "moc_batch_create": (C.c_int, [C.c_int, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]),
+    "moc_batch_destroy": (C.c_int, [C.c_void_p]),
+    "moc_batch_autotune": (C.c_int, [C.c_void_p]),
+    "moc_batch_set_width": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "moc_batch_widths": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
+    "moc_batch_sweep": (C.c_int, [C.c_void_p]),
+    "moc_batch_power_iterations": (C.c_int, [C.c_void_p, C.c_int, C.c_int, f64p]),
+    "moc_batch_results": (C.c_int, [C.c_void_p, f64p, f64p]),
+    "moc_batch_launch_count": (C.c_int64, [C.c_void_p]),
     "moc_renormalize_flux_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                                C.c_void_p, C.c_void_p, C.c_int64, C.c_int32,
                                                C.c_int32, C.c_int64, C.c_void_p, C.c_void_p]),

@@ -24,7 +24,7 @@ BUILD = PKG / "_build"
 LIB = PKG / "libsimplemoc_gb300.so"
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
-CU_SOURCES = ["moc_api.cu", "moc_sweep.cu", "moc_post.cu", "moc_refabi.cu"]
+CU_SOURCES = ["moc_api.cu", "moc_sweep.cu", "moc_post.cu", "moc_refabi.cu", "moc_batch.cu"]
 CPP_SOURCES = ["moc_host.cpp"]
 
 

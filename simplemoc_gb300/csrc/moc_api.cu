@@ -170,6 +170,7 @@ int upload_all(moc_problem *p, const moc_host *h) {
     p->launches += 4;
   }
   p->psi_pending = false;
+  TRY(moc_reset_psi_scale(p));
   TRY(moc_detect_psi_b(p));
   MOC_CUDA_TRY(cudaMemsetAsync(p->err, 0, sizeof(int32_t), p->stream));
   return MOC_OK;
@@ -221,9 +222,14 @@ int read_scalars(moc_problem *p, double *out) {
 }
 
 int sweep_impl(moc_problem *p) {
+  const bool had_pending = p->psi_pending && p->mode != MOC_MODE_FP64;
   int rc = moc_launch_sweep(p);
   if (rc != MOC_OK) return fail(p, rc);
-  if (p->mode != MOC_MODE_FP64) p->psi_pending = false;   // the sweep applied it
+  if (had_pending) {                   // the sweep applied it
+    p->psi_pending = false;
+    rc = moc_reset_psi_scale(p);
+    if (rc != MOC_OK) return fail(p, rc);
+  }
   if (p->mode == MOC_MODE_MIXED && (p->flags & MOC_FLAG_COMPENSATED) && p->phi_lo) {
     fold_kernel<<<1024, 256, 0, p->stream>>>(p->phi, p->phi_lo, p->nfsr * p->ldg);
     p->launches++;

@@ -1,0 +1,371 @@
+// moc_batch.cu -- many independent problems ("cores") swept by one persistent
+// launch, and their power iteration replayed as a CUDA graph.
+//
+// Each core keeps its own storage and post-sweep scalars (a moc_problem).  The
+// batch owns the task list of the persistent sweep: (core, first track) pairs of
+// 32/tpw tracks each, with the cores of the largest work per task first, and
+// one threads-per-track width per core, measured by moc_batch_autotune for
+// every distinct (segments per track, groups, polar angles, mode) key.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+#include <map>
+#include <mutex>
+#include <numeric>
+#include <tuple>
+#include <vector>
+
+#include "moc_internal.h"
+
+struct moc_batch {
+  std::vector<moc_problem *> cores;
+  int device = 0;
+  int mode = MOC_MODE_PLAIN;
+  bool quad = true;
+  cudaStream_t stream = nullptr;
+  SweepArgs *d_args = nullptr;
+  int2 *d_tasks = nullptr;
+  int *d_tpw = nullptr;
+  unsigned long long *d_counter = nullptr;
+  int64_t n_tasks = 0;
+  std::vector<int> tpw;
+  const float2 *table = nullptr;
+  int table_n = 0;
+  cudaGraphExec_t exec = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  int64_t launches = 0;
+};
+
+namespace {
+
+struct WidthKey {
+  int S, G, P, mode, axial;
+  bool operator<(const WidthKey &o) const {
+    return std::tie(S, G, P, mode, axial) < std::tie(o.S, o.G, o.P, o.mode, o.axial);
+  }
+};
+std::mutex g_width_mu;
+std::map<WidthKey, int> g_width_cache;
+
+int default_width(const moc_problem *p) {
+  const int nchunk = p->ldg / 4;
+  int w = 4;
+  while (w < nchunk) w <<= 1;
+  return w;
+}
+
+// Builds the per-core sweep arguments and the cost-ordered task list.
+int rebuild_tasks(moc_batch *b) {
+  const int n = (int)b->cores.size();
+  std::vector<SweepArgs> args((size_t)n);
+  for (int c = 0; c < n; ++c) {
+    moc_problem *p = b->cores[(size_t)c];
+    args[(size_t)c] = moc_sweep_args(p);
+    // the factor is 1 whenever no renormalisation is pending (see moc_reset_psi_scale)
+    args[(size_t)c].psi_scale = p->psi_scale;
+  }
+  std::vector<int> order((size_t)n);
+  std::iota(order.begin(), order.end(), 0);
+  auto cost = [&](int c) {
+    const moc_problem *p = b->cores[(size_t)c];
+    return (double)(32 / b->tpw[(size_t)c]) * p->d.n_seg * p->ldg;
+  };
+  std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return cost(x) > cost(y); });
+  std::vector<int2> tasks;
+  for (int c : order) {
+    const int gpw = 32 / b->tpw[(size_t)c];
+    for (int64_t t = 0; t < b->cores[(size_t)c]->n3d; t += gpw) tasks.push_back(make_int2(c, (int)t));
+  }
+  if (b->d_tasks) cudaFree(b->d_tasks);
+  b->d_tasks = nullptr;
+  b->n_tasks = (int64_t)tasks.size();
+  MOC_CUDA_TRY(cudaMalloc(&b->d_tasks, sizeof(int2) * (tasks.empty() ? 1 : tasks.size())));
+  MOC_CUDA_TRY(cudaMemcpy(b->d_tasks, tasks.data(), sizeof(int2) * tasks.size(), cudaMemcpyHostToDevice));
+  MOC_CUDA_TRY(cudaMemcpy(b->d_args, args.data(), sizeof(SweepArgs) * (size_t)n, cudaMemcpyHostToDevice));
+  MOC_CUDA_TRY(cudaMemcpy(b->d_tpw, b->tpw.data(), sizeof(int) * (size_t)n, cudaMemcpyHostToDevice));
+  if (b->exec) {
+    cudaGraphExecDestroy(b->exec);
+    cudaGraphDestroy(b->graph);
+    b->exec = nullptr;
+    b->graph = nullptr;
+  }
+  return MOC_OK;
+}
+
+// One batched sweep on b->stream (no host synchronisation).
+int batch_sweep(moc_batch *b) {
+  int rc = moc_launch_sweep_batch(b->device, b->stream, b->mode, b->quad, b->d_args, b->d_tasks,
+                                  b->n_tasks, b->d_tpw, b->d_counter, b->table, b->table_n);
+  if (rc != MOC_OK) return rc;
+  b->launches += 2;
+  for (moc_problem *p : b->cores) {
+    cudaStream_t own = p->stream;
+    p->stream = b->stream;
+    rc = moc_reset_psi_scale(p);
+    p->stream = own;
+    p->psi_pending = false;
+    if (rc != MOC_OK) return rc;
+  }
+  return MOC_OK;
+}
+
+// renormalize + update_sources + keff of every core on b->stream, k_eff chained
+// on the device.
+int batch_post(moc_batch *b) {
+  for (moc_problem *p : b->cores) {
+    cudaStream_t own = p->stream;
+    p->stream = b->stream;
+    int rc = moc_launch_renormalize(p);
+    if (rc == MOC_OK) rc = moc_launch_update(p, 0.0, true, true);
+    p->stream = own;
+    if (rc != MOC_OK) return rc;
+  }
+  return MOC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int moc_batch_create(int n, moc_problem *const *problems, moc_batch **out) {
+  if (n < 1 || !problems || !out) return MOC_ERR_ARG;
+  *out = nullptr;
+  moc_batch *b = new moc_batch();
+  b->cores.assign(problems, problems + n);
+  const moc_problem *p0 = problems[0];
+  if (!p0) {
+    delete b;
+    return MOC_ERR_ARG;
+  }
+  b->device = p0->device;
+  b->mode = p0->mode;
+  b->quad = p0->d.axial_exp == 2;
+  for (moc_problem *p : b->cores) {
+    // one launch: same device, mode, source order and (PLAIN) exponential table
+    if (!p || p->status != MOC_OK || p->device != b->device || p->mode != b->mode ||
+        (p->d.axial_exp == 2) != b->quad || p->ldg > 128 || p->mode == MOC_MODE_FP64 ||
+        (p->mode == MOC_MODE_MIXED && (p->flags & MOC_FLAG_COMPENSATED)) ||
+        p->d.table_n != p0->d.table_n || p->d.table_dx != p0->d.table_dx ||
+        p->d.table_maxval != p0->d.table_maxval) {
+      delete b;
+      return MOC_ERR_ARG;
+    }
+  }
+  cudaSetDevice(b->device);
+  b->table = reinterpret_cast<const float2 *>(p0->table);
+  b->table_n = p0->d.table_n;
+  for (moc_problem *p : b->cores) b->tpw.push_back(default_width(p));
+  int rc = MOC_OK;
+  if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&b->ev0) != cudaSuccess || cudaEventCreate(&b->ev1) != cudaSuccess ||
+      cudaMalloc(&b->d_args, sizeof(SweepArgs) * (size_t)n) != cudaSuccess ||
+      cudaMalloc(&b->d_tpw, sizeof(int) * (size_t)n) != cudaSuccess ||
+      cudaMalloc(&b->d_counter, sizeof(unsigned long long)) != cudaSuccess)
+    rc = MOC_ERR_CUDA;
+  // make every core's previous work visible to the batch stream
+  for (moc_problem *p : b->cores)
+    if (rc == MOC_OK && cudaStreamSynchronize(p->stream) != cudaSuccess) rc = MOC_ERR_CUDA;
+  if (rc == MOC_OK) rc = rebuild_tasks(b);
+  if (rc != MOC_OK) {
+    moc_batch_destroy(b);
+    return rc;
+  }
+  *out = b;
+  return MOC_OK;
+}
+
+int moc_batch_destroy(moc_batch *b) {
+  if (!b) return MOC_ERR_ARG;
+  cudaSetDevice(b->device);
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  if (b->d_args) cudaFree(b->d_args);
+  if (b->d_tasks) cudaFree(b->d_tasks);
+  if (b->d_tpw) cudaFree(b->d_tpw);
+  if (b->d_counter) cudaFree(b->d_counter);
+  if (b->ev0) cudaEventDestroy(b->ev0);
+  if (b->ev1) cudaEventDestroy(b->ev1);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+  return MOC_OK;
+}
+
+int moc_batch_set_width(moc_batch *b, int core, int threads_per_track) {
+  if (!b || core < 0 || core >= (int)b->cores.size()) return MOC_ERR_ARG;
+  const int w = threads_per_track;
+  if (w != 4 && w != 8 && w != 16 && w != 32) return MOC_ERR_ARG;
+  if (w * 4 < b->cores[(size_t)core]->ldg) return MOC_ERR_ARG;
+  b->tpw[(size_t)core] = w;
+  cudaSetDevice(b->device);
+  return rebuild_tasks(b);
+}
+
+int moc_batch_widths(const moc_batch *b, int *threads_per_track) {
+  if (!b || !threads_per_track) return MOC_ERR_ARG;
+  std::copy(b->tpw.begin(), b->tpw.end(), threads_per_track);
+  return MOC_OK;
+}
+
+// Autotuner of the batch: for every distinct key, times the persistent kernel on
+// up to 65536 tracks of one core of that key for each width that covers its
+// groups, with scratch tallies and angular fluxes (the state is untouched).
+int moc_batch_autotune(moc_batch *b) {
+  if (!b) return MOC_ERR_ARG;
+  cudaSetDevice(b->device);
+  const int n = (int)b->cores.size();
+  std::map<WidthKey, int> chosen;
+  for (int c = 0; c < n; ++c) {
+    moc_problem *p = b->cores[(size_t)c];
+    const WidthKey key{p->d.n_seg, p->d.n_groups, p->d.n_polar, p->mode, p->d.axial_exp};
+    {
+      std::lock_guard<std::mutex> lock(g_width_mu);
+      auto it = g_width_cache.find(key);
+      if (it != g_width_cache.end()) {
+        b->tpw[(size_t)c] = it->second;
+        continue;
+      }
+    }
+    if (chosen.count(key)) {
+      b->tpw[(size_t)c] = chosen[key];
+      continue;
+    }
+    const int64_t nsub = p->n3d < 65536 ? p->n3d : 65536;
+    float *phi_s = nullptr, *psi_s = nullptr;
+    SweepArgs *d_a = nullptr;
+    int2 *d_t = nullptr;
+    int *d_w = nullptr;
+    const size_t phi_bytes = sizeof(float) * (size_t)(p->nfsr * p->ldg);
+    const size_t psi_bytes = sizeof(float) * (size_t)(nsub * p->ldg);
+    int rc = MOC_OK;
+    if (cudaMalloc(&phi_s, phi_bytes) != cudaSuccess || cudaMalloc(&psi_s, psi_bytes) != cudaSuccess ||
+        cudaMalloc(&d_a, sizeof(SweepArgs)) != cudaSuccess ||
+        cudaMalloc(&d_t, sizeof(int2) * (size_t)nsub) != cudaSuccess ||
+        cudaMalloc(&d_w, sizeof(int)) != cudaSuccess)
+      rc = MOC_ERR_OOM;
+    SweepArgs a = moc_sweep_args(p);
+    a.n3d = nsub;
+    a.phi = phi_s;
+    a.psi = psi_s;
+    a.psi_scale = nullptr;
+    if (rc == MOC_OK &&
+        (cudaMemset(phi_s, 0, phi_bytes) != cudaSuccess ||
+         cudaMemcpy(psi_s, p->psi_f, psi_bytes, cudaMemcpyDeviceToDevice) != cudaSuccess ||
+         cudaMemcpy(d_a, &a, sizeof a, cudaMemcpyHostToDevice) != cudaSuccess))
+      rc = MOC_ERR_CUDA;
+    double best = 1e30;
+    int bw = default_width(p);
+    for (int w = 4; w <= 32 && rc == MOC_OK; w <<= 1) {
+      if (w * 4 < p->ldg) continue;
+      const int gpw = 32 / w;
+      std::vector<int2> t;
+      for (int64_t k = 0; k < nsub; k += gpw) t.push_back(make_int2(0, (int)k));
+      if (cudaMemcpy(d_t, t.data(), sizeof(int2) * t.size(), cudaMemcpyHostToDevice) != cudaSuccess ||
+          cudaMemcpy(d_w, &w, sizeof(int), cudaMemcpyHostToDevice) != cudaSuccess) {
+        rc = MOC_ERR_CUDA;
+        break;
+      }
+      double tot = 0.0;
+      for (int r = 0; r < 3 && rc == MOC_OK; ++r) {
+        cudaEventRecord(b->ev0, b->stream);
+        rc = moc_launch_sweep_batch(b->device, b->stream, b->mode, b->quad, d_a, d_t,
+                                    (int64_t)t.size(), d_w, b->d_counter, b->table, b->table_n);
+        cudaEventRecord(b->ev1, b->stream);
+        if (rc == MOC_OK && cudaEventSynchronize(b->ev1) != cudaSuccess) rc = MOC_ERR_CUDA;
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, b->ev0, b->ev1);
+        if (r > 0) tot += ms;                      // first run is the warm-up
+      }
+      if (rc == MOC_OK && tot < best) {
+        best = tot;
+        bw = w;
+      }
+    }
+    cudaFree(phi_s);
+    cudaFree(psi_s);
+    cudaFree(d_a);
+    cudaFree(d_t);
+    cudaFree(d_w);
+    if (rc != MOC_OK) return rc;
+    chosen[key] = bw;
+    b->tpw[(size_t)c] = bw;
+    std::lock_guard<std::mutex> lock(g_width_mu);
+    g_width_cache[key] = bw;
+  }
+  return rebuild_tasks(b);
+}
+
+int moc_batch_sweep(moc_batch *b) {
+  if (!b) return MOC_ERR_ARG;
+  cudaSetDevice(b->device);
+  int rc = batch_sweep(b);
+  if (rc != MOC_OK) return rc;
+  MOC_CUDA_TRY(cudaStreamSynchronize(b->stream));
+  return MOC_OK;
+}
+
+// `iters` power iterations of every core: the batched sweep, then each core's
+// renormalize / update_sources / compute_keff, k_eff chained on the device.
+// With use_graph the iteration is captured once as a CUDA graph and replayed.
+int moc_batch_power_iterations(moc_batch *b, int iters, int use_graph, double *ms_total) {
+  if (!b || iters < 1) return MOC_ERR_ARG;
+  cudaSetDevice(b->device);
+  int rc = MOC_OK;
+  if (use_graph && !b->exec) {
+    // one eager iteration first: kernel attributes are set and every core has
+    // a pending renormalisation, the steady state the graph replays
+    rc = batch_sweep(b);
+    if (rc == MOC_OK) rc = batch_post(b);
+    if (rc != MOC_OK) return rc;
+    MOC_CUDA_TRY(cudaStreamSynchronize(b->stream));
+    if (cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+      return MOC_ERR_CUDA;
+    rc = batch_sweep(b);
+    if (rc == MOC_OK) rc = batch_post(b);
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+    if (rc != MOC_OK || e != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      return rc != MOC_OK ? rc : MOC_ERR_CUDA;
+    }
+    b->graph = g;
+    if (cudaGraphInstantiate(&b->exec, g, 0) != cudaSuccess) return MOC_ERR_CUDA;
+  }
+  cudaEventRecord(b->ev0, b->stream);
+  for (int i = 0; i < iters && rc == MOC_OK; ++i) {
+    if (use_graph) {
+      if (cudaGraphLaunch(b->exec, b->stream) != cudaSuccess) rc = MOC_ERR_CUDA;
+      b->launches++;
+    } else {
+      rc = batch_sweep(b);
+      if (rc == MOC_OK) rc = batch_post(b);
+    }
+  }
+  cudaEventRecord(b->ev1, b->stream);
+  if (rc != MOC_OK) return rc;
+  MOC_CUDA_TRY(cudaEventSynchronize(b->ev1));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, b->ev0, b->ev1);
+  if (ms_total) *ms_total = ms;
+  for (moc_problem *p : b->cores) p->psi_pending = true;   // the last step renormalised
+  return MOC_OK;
+}
+
+int moc_batch_results(moc_batch *b, double *keff, double *residual) {
+  if (!b) return MOC_ERR_ARG;
+  cudaSetDevice(b->device);
+  MOC_CUDA_TRY(cudaStreamSynchronize(b->stream));
+  for (size_t c = 0; c < b->cores.size(); ++c) {
+    double sc[SC_COUNT];
+    MOC_CUDA_TRY(cudaMemcpy(sc, b->cores[c]->scalars, sizeof sc, cudaMemcpyDeviceToHost));
+    if (keff) keff[c] = sc[SC_KEFF];
+    if (residual) residual[c] = sc[SC_RESIDUAL];
+  }
+  return MOC_OK;
+}
+
+int64_t moc_batch_launch_count(const moc_batch *b) { return b ? b->launches : 0; }
+
+}  // extern "C"

@@ -98,6 +98,11 @@ struct moc_problem {
 int moc_launch_sweep(moc_problem *p);
 int moc_launch_sweep_csr(moc_problem *p, const int64_t *off, const float *ds, const float *z,
                          const int32_t *src);
+SweepArgs moc_sweep_args(moc_problem *p);
+int moc_launch_sweep_batch(int device, cudaStream_t st, int mode, bool quad, const SweepArgs *args,
+                           const int2 *tasks, int64_t n_tasks, const int *tpw,
+                           unsigned long long *counter, const float2 *table, int table_n);
+int moc_reset_psi_scale(moc_problem *p);
 int moc_sweep_launch_shape(const moc_problem *p, int *tpw, int *cpl);
 int moc_sweep_autotune(moc_problem *p, int64_t n_sub, int *tpw, int *cpl, double *ms);
 int moc_launch_renormalize(moc_problem *p);

@@ -457,9 +457,15 @@ int update_t(moc_problem *p, const T *phi, T *q, bool with_keff) {
   if (sizeof(T) == 4 && p->upd_items && p->ldg <= 128) {
     const size_t smem = sizeof(float) * ((size_t)d.n_groups * p->ldg +
                                          (size_t)UT_WARPS * d.n_groups * UT_ROWS);
-    if (smem > 48 * 1024)
+    // the attribute is set outside any stream capture: the first call of a
+    // process raises it to the largest size the kernel can take
+    static bool attr_set = false;
+    if (!attr_set) {
       MOC_CUDA_TRY(cudaFuncSetAttribute(update_tiled_kernel,
-                                        cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)(sizeof(float) * (128 * 128 + UT_WARPS * 128 * UT_ROWS))));
+      attr_set = true;
+    }
     update_tiled_kernel<<<RBLOCKS, RTHREADS, smem, p->stream>>>(
         reinterpret_cast<const float *>(phi), reinterpret_cast<float *>(q), p->xs_order,
         p->upd_items, p->n_upd_items, p->xs, p->scatter_t, d.fai, d.n_groups, p->ldg,
@@ -499,6 +505,19 @@ int keff_t(moc_problem *p, const T *phi) {
 
 int moc_post_scratch_blocks() { return RBLOCKS; }
 
+__global__ void set_float(float *dst, float v) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) *dst = v;
+}
+
+// The device factor is 1 whenever no renormalisation is pending, so that a
+// kernel may apply it unconditionally (the batched sweep does).
+int moc_reset_psi_scale(moc_problem *p) {
+  set_float<<<1, 32, 0, p->stream>>>(p->psi_scale, 1.0f);
+  MOC_CUDA_TRY(cudaGetLastError());
+  p->launches++;
+  return MOC_OK;
+}
+
 int moc_psi_materialize(moc_problem *p) {
   if (!p->psi_pending) return MOC_OK;
   int sms = 0;
@@ -508,7 +527,7 @@ int moc_psi_materialize(moc_problem *p) {
   MOC_CUDA_TRY(cudaGetLastError());
   p->launches++;
   p->psi_pending = false;
-  return MOC_OK;
+  return moc_reset_psi_scale(p);
 }
 
 int moc_detect_psi_b(moc_problem *p) {

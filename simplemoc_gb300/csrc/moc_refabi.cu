@@ -518,8 +518,12 @@ int sweep_ref(int64_t *segments) {
   MOC_CUDA_TRY(cudaMemcpyAsync(r.d_off + r.n3d, &M, sizeof(int64_t), cudaMemcpyHostToDevice, st));
   ref_expand<1><<<grid, 128, 0, st>>>(make_args(r, r.d_z));
   MOC_CUDA_TRY(cudaGetLastError());
+  const bool had_pending = r.p->psi_pending;
   RTRY(moc_launch_sweep_csr(r.p, r.d_off, r.d_sds, r.d_sz, r.d_ssrc));
-  r.p->psi_pending = false;   // the sweep applied any pending renormalisation
+  if (had_pending) {          // the sweep applied the pending renormalisation
+    r.p->psi_pending = false;
+    RTRY(moc_reset_psi_scale(r.p));
+  }
   MOC_CUDA_TRY(cudaStreamSynchronize(st));
   r.p->launches += 2;
   r.sweeps++;

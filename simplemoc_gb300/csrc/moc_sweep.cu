@@ -227,8 +227,8 @@ struct Rows {
   float4 v[CPL][QUAD ? 3 : 1];
 };
 
-template <int TPW, int CPL, bool QUAD>
-__device__ __forceinline__ void load_rows(const SweepArgs &a, const Seg &g, int li,
+template <int CPL, bool QUAD>
+__device__ __forceinline__ void load_rows(const SweepArgs &a, const Seg &g, int li, int TPW,
                                           Rows<CPL, QUAD> &r) {
 #pragma unroll
   for (int k = 0; k < CPL; ++k) {
@@ -256,6 +256,181 @@ __device__ __forceinline__ int checked_source(const SweepArgs &a, int s, int li)
 // traversal's sub-segments, csr_off/csr_ds/csr_z/csr_src) with the start height
 // of every sub-segment given; otherwise every track has S segments and its
 // height advances by ds*mu.  CSR runs one track per warp (TPW == 32).
+// One 3D track (or one group of TPW lanes' track) of the sweep.  TPW_CT is
+// the threads per track when known at compile time; 0 takes tpw_rt (the
+// batched kernel, where each core has its own width).
+template <int TPW_CT, int CPL, int MODE, bool QUAD, bool CSR>
+__device__ __forceinline__ void sweep_track(const SweepArgs &a, int64_t track, int lane,
+                                            int tpw_rt, const float2 *s_table) {
+  const int TPW = TPW_CT ? TPW_CT : tpw_rt;
+  const int li = lane % TPW;
+  const int64_t PZ = (int64_t)a.P * a.Z;
+  const bool valid = track < a.n3d;
+  const int64_t tr = valid ? track : a.n3d - 1;
+  const int64_t i2 = tr / PZ;
+  const int j = (int)((tr / a.Z) % a.P);
+  const float mu = a.mu[j];
+  const float mu2 = __fmul_rn(mu, mu);
+  const float w = a.weight[tr];
+  const float w_mu = __fmul_rn(w, mu);
+  float z;
+  int S;
+  const float *dsb;
+  const int32_t *srcb;
+  const float *zb = nullptr;
+  if (CSR) {
+    const int64_t o0 = a.csr_off[tr];
+    S = (int)(a.csr_off[tr + 1] - o0);
+    dsb = a.csr_ds + o0;
+    srcb = a.csr_src + o0;
+    zb = a.csr_z + o0;
+    z = 0.f;
+  } else {
+    S = a.S;
+    z = a.z0[tr];
+    dsb = a.seg_ds + (i2 * a.P + j) * S;
+    srcb = a.seg_src + tr * S;
+  }
+
+  float4 psi[CPL];
+#pragma unroll
+  for (int k = 0; k < CPL; ++k) {
+    const int c = li + TPW * k;
+    psi[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (c < a.nchunk) psi[k] = *reinterpret_cast<const float4 *>(a.psi + tr * a.ldg + 4 * c);
+    if (a.psi_scale) {                    // renormalisation still to apply (src/solver.c:1224)
+      const float sc = *a.psi_scale;
+      psi[k].x = __fmul_rn(psi[k].x, sc);
+      psi[k].y = __fmul_rn(psi[k].y, sc);
+      psi[k].z = __fmul_rn(psi[k].z, sc);
+      psi[k].w = __fmul_rn(psi[k].w, sc);
+    }
+  }
+
+  // segment streams: the current chunk of TPW entries and the next one
+  float ds_c = li < S ? __ldg(dsb + li) : 0.f;
+  int src_c = li < S ? __ldg(srcb + li) : 0;
+  float ds_n = TPW + li < S ? __ldg(dsb + TPW + li) : 0.f;
+  int src_n = TPW + li < S ? __ldg(srcb + TPW + li) : 0;
+  float z_c = 0.f, z_n = 0.f;
+  if (CSR) {
+    z_c = li < S ? __ldg(zb + li) : 0.f;
+    z_n = TPW + li < S ? __ldg(zb + TPW + li) : 0.f;
+    z = __shfl_sync(FULL, z_c, 0, TPW);
+  }
+
+  float ds = __shfl_sync(FULL, ds_c, 0, TPW);
+  Seg g = segment_geometry(a, z, checked_source(a, __shfl_sync(FULL, src_c, 0, TPW), li));
+  Rows<CPL, QUAD> rows;
+  if (S > 0) load_rows<CPL, QUAD>(a, g, li, TPW, rows);
+
+  for (int n = 0; n < S; ++n) {
+    float z_next = CSR ? 0.f : advance_z(a, z, ds, mu);
+    // ---- issue the loads of segment n+1 before the arithmetic of segment n
+    float ds1 = 0.f;
+    Seg g1 = g;
+    Rows<CPL, QUAD> rows1 = rows;
+    const int m = n + 1;
+    if (m < S) {
+      const int k = m & (TPW - 1);
+      if (k == 0) {
+        ds_c = ds_n;
+        src_c = src_n;
+        const int nl = m + TPW + li;
+        ds_n = nl < S ? __ldg(dsb + nl) : 0.f;
+        src_n = nl < S ? __ldg(srcb + nl) : 0;
+        if (CSR) {
+          z_c = z_n;
+          z_n = nl < S ? __ldg(zb + nl) : 0.f;
+        }
+      }
+      if (CSR) z_next = __shfl_sync(FULL, z_c, k, TPW);
+      ds1 = __shfl_sync(FULL, ds_c, k, TPW);
+      g1 = segment_geometry(a, z_next, checked_source(a, __shfl_sync(FULL, src_c, k, TPW), li));
+      load_rows<CPL, QUAD>(a, g1, li, TPW, rows1);
+    }
+    // ---- segment n
+#pragma unroll
+    for (int k = 0; k < CPL; ++k) {
+      const int c = li + TPW * k;
+      if (c >= a.nchunk) continue;
+      const int g4 = 4 * c;
+      const float *cf = a.coef + g.crow + g4;
+      const float4 sig = __ldg(reinterpret_cast<const float4 *>(cf));
+      const float4 r1 = __ldg(reinterpret_cast<const float4 *>(cf + 4 * a.ldg));
+      float4 t;
+      if (QUAD) {
+        const float4 y1 = rows.v[k][0];
+        const float4 y2 = rows.v[k][QUAD ? 1 : 0];
+        const float4 y3 = rows.v[k][QUAD ? 2 : 0];
+        if (MODE == MODE_PLAIN) {
+          const float4 r2 = __ldg(reinterpret_cast<const float4 *>(cf + 5 * a.ldg));
+          const float4 r3 = __ldg(reinterpret_cast<const float4 *>(cf + 6 * a.ldg));
+          const float4 r4 = __ldg(reinterpret_cast<const float4 *>(cf + 7 * a.ldg));
+#pragma unroll
+          for (int e = 0; e < 4; ++e) {
+            // the reference's divisors, formed with its own operations
+            const float sg = get(sig, e);
+            const float sg2 = __fmul_rn(sg, sg);                        // solver.c:153
+            const float sg3 = __fmul_rn(sg, sg2);                       // solver.c:176
+            const float sg4 = __fmul_rn(__fmul_rn(3.f, sg2), sg2);      // solver.c:198
+            float p = get(psi[k], e);
+            set(t, e, plain_quad(a, s_table, get(y1, e), get(y2, e), get(y3, e), sg, sg2, sg3,
+                                 sg4, get(r1, e), get(r2, e), get(r3, e), get(r4, e), g.zin,
+                                 ds, mu, mu2, w, p));
+            set(psi[k], e, p);
+          }
+        } else {
+#pragma unroll
+          for (int e = 0; e < 4; ++e) {
+            const float q1r = get(r1, e);
+            const float q2r = q1r * q1r;
+            float p = get(psi[k], e);
+            set(t, e, mixed_quad(a, get(y1, e), get(y2, e), get(y3, e), get(sig, e), q1r, q2r,
+                                 q1r * q2r, q2r * q2r * (1.0f / 3.0f), g.zin, ds, mu, mu2, w,
+                                 p));
+            set(psi[k], e, p);
+          }
+        }
+      } else {
+        const float4 y = rows.v[k][0];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          float p = get(psi[k], e);
+          if (MODE == MODE_PLAIN)
+            set(t, e, plain_flat(a, s_table, get(y, e), get(sig, e), get(r1, e), ds, w_mu, p));
+          else
+            set(t, e, mixed_flat(get(y, e), get(sig, e), get(r1, e), ds, w_mu, p));
+          set(psi[k], e, p);
+        }
+      }
+      if (valid) {
+        float *dst = a.phi + g.frow + g4;
+        if (MODE == MODE_MIXED && a.phi_lo != nullptr) {
+          float *lo = a.phi_lo + g.frow + g4;
+          comp_add(dst + 0, lo + 0, t.x);
+          comp_add(dst + 1, lo + 1, t.y);
+          comp_add(dst + 2, lo + 2, t.z);
+          comp_add(dst + 3, lo + 3, t.w);
+        } else {
+          red_add_v4(dst, t.x, t.y, t.z, t.w);
+        }
+      }
+    }
+    z = z_next;
+    ds = ds1;
+    g = g1;
+    rows = rows1;
+  }
+  if (valid) {
+#pragma unroll
+    for (int k = 0; k < CPL; ++k) {
+      const int c = li + TPW * k;
+      if (c < a.nchunk) *reinterpret_cast<float4 *>(a.psi + tr * a.ldg + 4 * c) = psi[k];
+    }
+  }
+}
+
 template <int TPW, int CPL, int MODE, bool QUAD, bool CSR = false>
 __global__ void __launch_bounds__(BLOCK) sweep_kernel(SweepArgs a) {
   extern __shared__ float2 s_table[];
@@ -265,179 +440,42 @@ __global__ void __launch_bounds__(BLOCK) sweep_kernel(SweepArgs a) {
   }
   constexpr int GPW = 32 / TPW;
   const int lane = threadIdx.x & 31;
-  const int li = lane % TPW;
   const int gw = lane / TPW;
   const int64_t warp_id = ((int64_t)blockIdx.x * BLOCK + threadIdx.x) >> 5;
   const int64_t n_warps = ((int64_t)gridDim.x * BLOCK) >> 5;
-  const int64_t PZ = (int64_t)a.P * a.Z;
   static_assert(!CSR || TPW == 32, "variable-length streams run one track per warp");
+  for (int64_t base = warp_id * GPW; base < a.n3d; base += n_warps * GPW)
+    sweep_track<TPW, CPL, MODE, QUAD, CSR>(a, base + gw, lane, TPW, s_table);
+}
 
-  for (int64_t base = warp_id * GPW; base < a.n3d; base += n_warps * GPW) {
-    const int64_t track = base + gw;
-    const bool valid = track < a.n3d;
-    const int64_t tr = valid ? track : a.n3d - 1;
-    const int64_t i2 = tr / PZ;
-    const int j = (int)((tr / a.Z) % a.P);
-    const float mu = a.mu[j];
-    const float mu2 = __fmul_rn(mu, mu);
-    const float w = a.weight[tr];
-    const float w_mu = __fmul_rn(w, mu);
-    float z;
-    int S;
-    const float *dsb;
-    const int32_t *srcb;
-    const float *zb = nullptr;
-    if (CSR) {
-      const int64_t o0 = a.csr_off[tr];
-      S = (int)(a.csr_off[tr + 1] - o0);
-      dsb = a.csr_ds + o0;
-      srcb = a.csr_src + o0;
-      zb = a.csr_z + o0;
-      z = 0.f;
-    } else {
-      S = a.S;
-      z = a.z0[tr];
-      dsb = a.seg_ds + (i2 * a.P + j) * S;
-      srcb = a.seg_src + tr * S;
-    }
-
-    float4 psi[CPL];
-#pragma unroll
-    for (int k = 0; k < CPL; ++k) {
-      const int c = li + TPW * k;
-      psi[k] = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (c < a.nchunk) psi[k] = *reinterpret_cast<const float4 *>(a.psi + tr * a.ldg + 4 * c);
-      if (a.psi_scale) {                    // renormalisation still to apply (src/solver.c:1224)
-        const float sc = *a.psi_scale;
-        psi[k].x = __fmul_rn(psi[k].x, sc);
-        psi[k].y = __fmul_rn(psi[k].y, sc);
-        psi[k].z = __fmul_rn(psi[k].z, sc);
-        psi[k].w = __fmul_rn(psi[k].w, sc);
-      }
-    }
-
-    // segment streams: the current chunk of TPW entries and the next one
-    float ds_c = li < S ? __ldg(dsb + li) : 0.f;
-    int src_c = li < S ? __ldg(srcb + li) : 0;
-    float ds_n = TPW + li < S ? __ldg(dsb + TPW + li) : 0.f;
-    int src_n = TPW + li < S ? __ldg(srcb + TPW + li) : 0;
-    float z_c = 0.f, z_n = 0.f;
-    if (CSR) {
-      z_c = li < S ? __ldg(zb + li) : 0.f;
-      z_n = TPW + li < S ? __ldg(zb + TPW + li) : 0.f;
-      z = __shfl_sync(FULL, z_c, 0, TPW);
-    }
-
-    float ds = __shfl_sync(FULL, ds_c, 0, TPW);
-    Seg g = segment_geometry(a, z, checked_source(a, __shfl_sync(FULL, src_c, 0, TPW), li));
-    Rows<CPL, QUAD> rows;
-    if (S > 0) load_rows<TPW, CPL, QUAD>(a, g, li, rows);
-
-    for (int n = 0; n < S; ++n) {
-      float z_next = CSR ? 0.f : advance_z(a, z, ds, mu);
-      // ---- issue the loads of segment n+1 before the arithmetic of segment n
-      float ds1 = 0.f;
-      Seg g1 = g;
-      Rows<CPL, QUAD> rows1 = rows;
-      const int m = n + 1;
-      if (m < S) {
-        const int k = m & (TPW - 1);
-        if (k == 0) {
-          ds_c = ds_n;
-          src_c = src_n;
-          const int nl = m + TPW + li;
-          ds_n = nl < S ? __ldg(dsb + nl) : 0.f;
-          src_n = nl < S ? __ldg(srcb + nl) : 0;
-          if (CSR) {
-            z_c = z_n;
-            z_n = nl < S ? __ldg(zb + nl) : 0.f;
-          }
-        }
-        if (CSR) z_next = __shfl_sync(FULL, z_c, k, TPW);
-        ds1 = __shfl_sync(FULL, ds_c, k, TPW);
-        g1 = segment_geometry(a, z_next, checked_source(a, __shfl_sync(FULL, src_c, k, TPW), li));
-        load_rows<TPW, CPL, QUAD>(a, g1, li, rows1);
-      }
-      // ---- segment n
-#pragma unroll
-      for (int k = 0; k < CPL; ++k) {
-        const int c = li + TPW * k;
-        if (c >= a.nchunk) continue;
-        const int g4 = 4 * c;
-        const float *cf = a.coef + g.crow + g4;
-        const float4 sig = __ldg(reinterpret_cast<const float4 *>(cf));
-        const float4 r1 = __ldg(reinterpret_cast<const float4 *>(cf + 4 * a.ldg));
-        float4 t;
-        if (QUAD) {
-          const float4 y1 = rows.v[k][0];
-          const float4 y2 = rows.v[k][QUAD ? 1 : 0];
-          const float4 y3 = rows.v[k][QUAD ? 2 : 0];
-          if (MODE == MODE_PLAIN) {
-            const float4 r2 = __ldg(reinterpret_cast<const float4 *>(cf + 5 * a.ldg));
-            const float4 r3 = __ldg(reinterpret_cast<const float4 *>(cf + 6 * a.ldg));
-            const float4 r4 = __ldg(reinterpret_cast<const float4 *>(cf + 7 * a.ldg));
-#pragma unroll
-            for (int e = 0; e < 4; ++e) {
-              // the reference's divisors, formed with its own operations
-              const float sg = get(sig, e);
-              const float sg2 = __fmul_rn(sg, sg);                        // solver.c:153
-              const float sg3 = __fmul_rn(sg, sg2);                       // solver.c:176
-              const float sg4 = __fmul_rn(__fmul_rn(3.f, sg2), sg2);      // solver.c:198
-              float p = get(psi[k], e);
-              set(t, e, plain_quad(a, s_table, get(y1, e), get(y2, e), get(y3, e), sg, sg2, sg3,
-                                   sg4, get(r1, e), get(r2, e), get(r3, e), get(r4, e), g.zin,
-                                   ds, mu, mu2, w, p));
-              set(psi[k], e, p);
-            }
-          } else {
-#pragma unroll
-            for (int e = 0; e < 4; ++e) {
-              const float q1r = get(r1, e);
-              const float q2r = q1r * q1r;
-              float p = get(psi[k], e);
-              set(t, e, mixed_quad(a, get(y1, e), get(y2, e), get(y3, e), get(sig, e), q1r, q2r,
-                                   q1r * q2r, q2r * q2r * (1.0f / 3.0f), g.zin, ds, mu, mu2, w,
-                                   p));
-              set(psi[k], e, p);
-            }
-          }
-        } else {
-          const float4 y = rows.v[k][0];
-#pragma unroll
-          for (int e = 0; e < 4; ++e) {
-            float p = get(psi[k], e);
-            if (MODE == MODE_PLAIN)
-              set(t, e, plain_flat(a, s_table, get(y, e), get(sig, e), get(r1, e), ds, w_mu, p));
-            else
-              set(t, e, mixed_flat(get(y, e), get(sig, e), get(r1, e), ds, w_mu, p));
-            set(psi[k], e, p);
-          }
-        }
-        if (valid) {
-          float *dst = a.phi + g.frow + g4;
-          if (MODE == MODE_MIXED && a.phi_lo != nullptr) {
-            float *lo = a.phi_lo + g.frow + g4;
-            comp_add(dst + 0, lo + 0, t.x);
-            comp_add(dst + 1, lo + 1, t.y);
-            comp_add(dst + 2, lo + 2, t.z);
-            comp_add(dst + 3, lo + 3, t.w);
-          } else {
-            red_add_v4(dst, t.x, t.y, t.z, t.w);
-          }
-        }
-      }
-      z = z_next;
-      ds = ds1;
-      g = g1;
-      rows = rows1;
-    }
-    if (valid) {
-#pragma unroll
-      for (int k = 0; k < CPL; ++k) {
-        const int c = li + TPW * k;
-        if (c < a.nchunk) *reinterpret_cast<float4 *>(a.psi + tr * a.ldg + 4 * c) = psi[k];
-      }
-    }
+// Batched sweep of many independent problems ("cores") in one persistent
+// launch.  Work = tasks (core, first track) of 32/tpw tracks each, ordered by
+// cost; every warp takes the next task from a global counter until none is
+// left (a work queue, not a wait).  Each core runs with its own threads per
+// track (tpw), so small group counts pack several tracks into a warp.
+template <int MODE, bool QUAD>
+__global__ void __launch_bounds__(BLOCK) sweep_batch_kernel(const SweepArgs *__restrict__ cores,
+                                                            const int2 *__restrict__ tasks,
+                                                            int64_t n_tasks,
+                                                            const int *__restrict__ core_tpw,
+                                                            unsigned long long *__restrict__ counter,
+                                                            const float2 *__restrict__ table,
+                                                            int table_n) {
+  extern __shared__ float2 s_table[];
+  if (MODE == MODE_PLAIN) {
+    for (int i = threadIdx.x; i < table_n; i += BLOCK) s_table[i] = table[i];
+    __syncthreads();
+  }
+  const int lane = threadIdx.x & 31;
+  for (;;) {
+    unsigned long long t = 0;
+    if (lane == 0) t = atomicAdd(counter, 1ull);
+    t = __shfl_sync(FULL, t, 0);
+    if (t >= (unsigned long long)n_tasks) break;
+    const int2 task = tasks[t];
+    const SweepArgs &a = cores[task.x];
+    const int tpw = core_tpw[task.x];
+    sweep_track<0, 1, MODE, QUAD, false>(a, (int64_t)task.y + lane / tpw, lane, tpw, s_table);
   }
 }
 
@@ -791,3 +829,30 @@ int moc_launch_sweep_csr(moc_problem *p, const int64_t *off, const float *ds, co
                          : launch_t<32, 4, MODE_MIXED, false, true>(p, a));
   return MOC_ERR_UNSUPPORTED;
 }
+
+// One persistent launch over the tasks of many problems (see sweep_batch_kernel).
+int moc_launch_sweep_batch(int device, cudaStream_t st, int mode, bool quad, const SweepArgs *args,
+                           const int2 *tasks, int64_t n_tasks, const int *tpw,
+                           unsigned long long *counter, const float2 *table, int table_n) {
+  if (mode == MOC_MODE_FP64) return MOC_ERR_UNSUPPORTED;
+  const bool plain = mode == MOC_MODE_PLAIN;
+  auto kern = plain ? (quad ? sweep_batch_kernel<MODE_PLAIN, true> : sweep_batch_kernel<MODE_PLAIN, false>)
+                    : (quad ? sweep_batch_kernel<MODE_MIXED, true> : sweep_batch_kernel<MODE_MIXED, false>);
+  const size_t smem = plain ? sizeof(float2) * (size_t)table_n : 0;
+  if (smem > 48 * 1024)
+    MOC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 0, sms = 0;
+  MOC_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BLOCK, smem));
+  MOC_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+  if (per_sm < 1) return MOC_ERR_UNSUPPORTED;
+  int64_t grid = (int64_t)per_sm * sms;
+  const int64_t need = (n_tasks + (BLOCK / 32) - 1) / (BLOCK / 32);
+  if (grid > need) grid = need;
+  if (grid < 1) grid = 1;
+  MOC_CUDA_TRY(cudaMemsetAsync(counter, 0, sizeof(unsigned long long), st));
+  kern<<<(unsigned)grid, BLOCK, smem, st>>>(args, tasks, n_tasks, tpw, counter, table, table_n);
+  MOC_CUDA_TRY(cudaGetLastError());
+  return MOC_OK;
+}
+
+SweepArgs moc_sweep_args(moc_problem *p) { return build_args(p); }

@@ -1,0 +1,88 @@
+"""GPU tests of the batched persistent sweep: every core of a batch against the
+same core swept on its own (and against the oracle), with and without the
+CUDA-graph power iteration.
+
+Tolerances as in test_gpu_sweep: psi bit-identical after one PLAIN sweep;
+fluxes normwise <= 1e-5 (tally order); k_eff <= 1e-5.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from tests._util import rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+def _specs():
+    import simplemoc_gb300 as sm
+    out = []
+    for c, (g, p, s, n2d, ns) in enumerate([(100, 4, 50, 24, 300), (20, 2, 80, 40, 150),
+                                            (37, 6, 20, 16, 200), (64, 4, 33, 20, 250),
+                                            (7, 2, 45, 12, 90), (128, 6, 26, 8, 120)]):
+        out.append(sm.ProblemSpec(n_groups=g, fai=5, cai=4, height=200.0, n_sources=ns,
+                                  n_tracks_2d=n2d, n_polar=p, z_stacked=10, n_seg=s,
+                                  seed=7000 + c))
+    return out
+
+
+@pytest.mark.parametrize("mode", ["plain", "mixed"])
+def test_batched_sweep_equals_separate_sweeps(gpu_available, port, mode):
+    import simplemoc_gb300 as sm
+    from simplemoc_gb300.batch import Batch
+    specs = _specs()
+    hps = [sm.generate(s) for s in specs]
+    solvers = [sm.Solver(h, mode=mode) for h in hps]
+    with Batch(solvers) as b:
+        widths = b.autotune()
+        assert all(w in (4, 8, 16, 32) for w in widths)
+        b.sweep()
+    for h, s, w in zip(hps, solvers, widths):
+        out = s.download(psi_f=True, fine_flux=True, fine_source=False)
+        with sm.Solver(h, mode=mode) as alone:
+            alone.transport_sweep()
+            ref = alone.download(psi_f=True, fine_flux=True, fine_source=False)
+        assert np.array_equal(out["psi_f"], ref["psi_f"]), (h.spec.n_groups, w)
+        assert rel_err(out["fine_flux"], ref["fine_flux"]) <= 1e-5
+        if mode == "plain":
+            st = oracle.fresh_state(h)
+            op = oracle.make_problem(h)
+            port.sweep(op, st["fine_source"], st["fine_flux"], st["psi_f"])
+            assert np.array_equal(out["psi_f"], st["psi_f"])
+        s.close()
+
+
+@pytest.mark.parametrize("graph", [True, False])
+def test_batched_power_iterations_match_separate_runs(gpu_available, graph):
+    import simplemoc_gb300 as sm
+    from simplemoc_gb300.batch import Batch
+    specs = _specs()
+    hps = [sm.generate(s) for s in specs]
+    solvers = [sm.Solver(h, mode="plain") for h in hps]
+    iters = 4
+    with Batch(solvers) as b:
+        b.power_iterations(iters, graph=graph)
+        keff, res = b.results()
+    for c, (h, s) in enumerate(zip(hps, solvers)):
+        # the graph path runs one eager iteration before its first capture
+        n_done = iters + (1 if graph else 0)
+        with sm.Solver(h, mode="plain") as alone:
+            hist = alone.run(n_done)
+            ref = alone.download(fine_flux=True, fine_source=True, psi_f=True)
+        out = s.download(fine_flux=True, fine_source=True, psi_f=True)
+        assert abs(keff[c] - hist[-1][0]) <= 1e-5 * abs(hist[-1][0]), c
+        for k in ("fine_flux", "fine_source", "psi_f"):
+            assert rel_err(out[k], ref[k]) <= 1e-5, (c, k)
+        s.close()
+
+
+def test_batch_rejects_mixed_modes(gpu_available):
+    import simplemoc_gb300 as sm
+    from simplemoc_gb300.batch import Batch
+    specs = _specs()[:2]
+    a = sm.Solver(sm.generate(specs[0]), mode="plain")
+    b = sm.Solver(sm.generate(specs[1]), mode="mixed")
+    with pytest.raises(sm.MocError):
+        Batch([a, b])
+    a.close()
+    b.close()
