@@ -44,7 +44,9 @@ def _args():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--config", choices=["default", "small", "default_1k"], default="default")
+    ap.add_argument("--config", choices=["default", "small", "default_1k", "batched", "adjoint"],
+                    default="default")
+    ap.add_argument("--cores", type=int, default=64, help="cores of the batched workload")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
@@ -226,9 +228,133 @@ def _traffic_from_profiles():
     return None
 
 
+def run_batched(args):
+    """The batched workload: independent small cores of uneven sizes swept in
+    one persistent launch per iteration, the power iteration replayed as a CUDA
+    graph.  value = integrations of all cores per second (MIXED, graph); the
+    same cores run one after the other through the single-problem path, and
+    the PLAIN batch, are reported beside it."""
+    import torch
+
+    import simplemoc_gb300 as sm
+    from simplemoc_gb300.batch import Batch, batched_specs
+    torch.cuda.set_device(0)
+    specs = batched_specs(args.cores)
+    hps = [sm.generate(s, with_state=False) for s in specs]
+    ints = sum(s.integrations_per_sweep for s in specs)
+    K, W = max(1, args.steps), max(0, args.warmup)
+    out = {}
+    for mode in ("mixed", "plain"):
+        solvers = [sm.Solver(h, mode=mode) for h in hps]
+        with Batch(solvers) as b:
+            widths = b.autotune()
+            b.power_iterations(max(1, W), graph=True)
+            with ClockSampler(0) as clk:
+                ms = b.power_iterations(K, graph=True)
+            keff, _ = b.results()
+        out[mode] = {"value": ints * K / (ms / 1e3), "ms_per_step": ms / K, "widths": widths,
+                     "clocks": clk.summary(), "keff_mean": float(np.mean(keff))}
+        # the same cores one after the other through the single-problem path
+        for s_ in solvers:
+            s_.power_iteration(1.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        tot = 0.0
+        for s_ in solvers:
+            r = s_.time_power_iterations(K)
+            tot += r["ms_total"]
+        out[mode]["sequential_value"] = ints * K / (tot / 1e3)
+        for s_ in solvers:
+            s_.close()
+    line = {
+        "metric": "segment-group integrations/s per sweep, chosen vs plain @ FSR flux rel err "
+                  "<=1e-5",
+        "value": out["mixed"]["value"], "unit": "integrations/s", "n_gpus": 1, "steps": K,
+        "warmup": W, "ms_per_step": out["mixed"]["ms_per_step"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {"workload": f"batched: {len(specs)} independent cores, "
+                               f"{sum(s.n_tracks_3d for s in specs)} 3D tracks, "
+                               f"{ints:.3e} integrations per iteration",
+                   "mode": "mixed", "step": "one power iteration of every core (CUDA graph)",
+                   "l2": "inputs larger than L2 (no flush)"},
+        "plain": {"value": out["plain"]["value"], "unit": "integrations/s"},
+        "chosen_vs_plain": out["mixed"]["value"] / out["plain"]["value"],
+        "sequential": {"mixed": out["mixed"]["sequential_value"],
+                       "plain": out["plain"]["sequential_value"]},
+        "batched_vs_sequential": out["mixed"]["value"] / out["mixed"]["sequential_value"],
+        "widths": out["mixed"]["widths"], "clocks": out["mixed"]["clocks"],
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_adjoint(args):
+    """The adjoint workload: the small problem's geometry with 40 groups, one
+    fixed-source sweep and its reverse sweep (psi checkpoints every 8
+    segments).  Reports forward, forward-with-checkpoints and reverse times
+    (events on the library stream, via the C ABI) and their ratio."""
+    import torch
+
+    import simplemoc_gb300 as sm
+    from simplemoc_gb300 import _lib as L
+    torch.cuda.set_device(0)
+    spec = sm.CONFIG_SMALL.with_(n_groups=40, seed=20260104)
+    hp = sm.generate(spec, with_state=False)
+    dev = torch.device("cuda", 0)
+    K, W = max(1, args.steps), max(0, args.warmup)
+    with sm.Solver(hp, mode="mixed") as s:
+        lib, h = s._lib, s.handle
+        shape = s.autotune()[:2]
+        s.time_sweep(max(1, W))
+        t_fwd = s.time_sweep(K)
+        dphi = torch.rand(spec.n_fsr * spec.n_groups, device=dev)
+        dq = torch.empty_like(dphi)
+        dsig = torch.empty(hp.sigt.size, dtype=torch.float64, device=dev)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        fw, rv = [], []
+        for it in range(W + K):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            L.check(lib.moc_adjoint_forward(h, 8), "moc_adjoint_forward")
+            s.synchronize()
+            t1 = time.perf_counter()
+            L.check(lib.moc_adjoint_backward(h, dphi.data_ptr(), dq.data_ptr(), dsig.data_ptr(),
+                                             None), "moc_adjoint_backward")
+            s.synchronize()
+            t2 = time.perf_counter()
+            if it >= W:
+                fw.append((t1 - t0) * 1e3)
+                rv.append((t2 - t1) * 1e3)
+    f, r = float(np.median(fw)), float(np.median(rv))
+    line = {
+        "metric": "adjoint sweep time / forward sweep time", "value": (f + r) / t_fwd,
+        "unit": "ratio", "n_gpus": 1, "steps": K, "warmup": W, "higher_is_better": False,
+        "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {"workload": f"adjoint: {spec.n_tracks_3d} tracks x {spec.n_seg} segments x "
+                               f"{spec.n_groups} groups, checkpoints every 8 segments"},
+        "forward_ms": t_fwd, "forward_with_checkpoints_ms": f, "reverse_ms": r,
+        "launch_shape": list(shape),
+        "integrations_per_s_forward": spec.integrations_per_sweep / (t_fwd / 1e3),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = _args()
     import simplemoc_gb300 as sm
+    if args.config == "adjoint":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable":
+                              "the reference has no adjoint sweep"}))
+            return
+        run_adjoint(args)
+        return
+    if args.config == "batched":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable":
+                              "the CPU arm times the default problem"}))
+            return
+        run_batched(args)
+        return
     spec = sm.CONFIGS[args.config]
     if args.impl == "reference":
         run_reference(args, spec)

@@ -201,6 +201,36 @@ int moc_time_power_iterations(moc_problem *p, int iters, double *ms_total,
 /* Number of kernels the library has launched on this handle so far. */
 int64_t moc_launch_count(const moc_problem *p);
 
+/* ---- state on device pointers (row stride n_groups) --------------------- */
+int moc_set_fine_source_device(moc_problem *p, const float *q);
+int moc_set_fine_source64_device(moc_problem *p, const double *q);  /* FP64 mode */
+/* Replaces the sigma_t table (host array [n_sigt*G]) and its coefficients. */
+int moc_set_sigma_t(moc_problem *p, const float *sigt);
+/* Zeroes the scalar flux (a fixed-source sweep tallies from zero) and/or the
+ * angular flux, in every precision held. */
+int moc_zero_state(moc_problem *p, int flux, int psi);
+int moc_get_fine_flux_device(moc_problem *p, float *phi);
+int moc_get_fine_flux64_device(moc_problem *p, double *phi);   /* FP64 mode */
+
+/* ---- adjoint sweep (no counterpart in the reference) ------------------- */
+/* Reverse-mode derivative of one transport sweep in the MIXED arithmetic
+ * (the PLAIN table is piecewise linear with jumps, not differentiable).
+ * moc_adjoint_forward runs the sweep (tallies added to the scalar flux, psi_f
+ * updated) and checkpoints the angular flux every k_ckpt (1..8) segments.
+ * moc_adjoint_backward takes dL/dphi for any loss L of the scalar flux (device
+ * array [NS*F*G]) and writes, on device arrays (NULL skips):
+ *   dq     [NS*F*G]       dL/d fine_source (the q0/q1/q2 fit rows)
+ *   dsigt  [n_sigt*G]     dL/d sigma_t, FP64
+ *   dpsi_in [N3D*G]       dL/d angular flux entering each track
+ * psi is recomputed from the checkpoints, not stored per segment. */
+int moc_adjoint_forward(moc_problem *p, int k_ckpt);
+int moc_adjoint_backward(moc_problem *p, const float *dphi, float *dq, double *dsigt,
+                         float *dpsi_in);
+/* Lanes per track (1..32, any width) and 4-group chunks per lane (1 or 2) of
+ * the reverse sweep; 0, 0 = automatic (ceil(G/4) lanes of one chunk up to 128
+ * groups).  MOC_ERR_ARG when lanes x chunks x 4 < G. */
+int moc_set_adjoint_width(moc_problem *p, int lanes_per_track, int chunks_per_lane);
+
 /* ---- batched sweep of independent problems ------------------------------ */
 /* Many independent problems ("cores", e.g. small reactor cores of different
  * sizes and group counts) on one device, swept by ONE persistent launch: warps
@@ -208,7 +238,7 @@ int64_t moc_launch_count(const moc_problem *p);
  * with its own threads per track.  The batch references the problems (they
  * stay owned by the caller and keep their own state); all must share the
  * device, mode (PLAIN or MIXED), source order and exponential table, and have
- * at most 128 groups. */
+ * at most 256 groups. */
 typedef struct moc_batch moc_batch;
 int moc_batch_create(int n, moc_problem *const *problems, moc_batch **out);
 int moc_batch_destroy(moc_batch *b);

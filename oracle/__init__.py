@@ -118,6 +118,7 @@ class Port:
             "oracle_compute_keff64": (C.c_double, [P, f64p, C.c_double]),
             "oracle_ref_sweep": (C.c_int64, [P, C.POINTER(OracleRefGeo), f32p, f32p, f32p, f32p,
                                              i32p]),
+            "oracle_adjoint64": (None, [P, f64p, f64p, f64p, f64p, f64p, f64p]),
         }
         for n, (r, a) in sig.items():
             fn = getattr(lib, n)
@@ -171,6 +172,20 @@ class Port:
     def sweep64(self, op, q, phi, psi_f) -> int:
         d = C.c_double
         return self.lib.oracle_sweep64(C.byref(op), _p(q, d), _p(phi, d), _p(psi_f, d))
+
+    def adjoint64(self, op, q, dphi, psi_in=None):
+        """(dq, dsigt, dpsi_in) of one FP64 sweep for dL/dphi (all float64)."""
+        d = C.c_double
+        G = op.G
+        nr = op.NS * op.F
+        n3d = op.N2D * op.P * op.Z
+        n_sigt = op._keep.sigt.size // G
+        dq = np.zeros(nr * G, np.float64)
+        ds = np.zeros(n_sigt * G, np.float64)
+        dp = np.zeros(n3d * G, np.float64)
+        self.lib.oracle_adjoint64(C.byref(op), _p(q, d), _p(psi_in, d), _p(dphi, d), _p(dq, d),
+                                  _p(ds, d), _p(dp, d))
+        return dq, ds, dp
 
     def renormalize64(self, op, phi, psi_f, psi_b) -> None:
         d = C.c_double

@@ -686,3 +686,136 @@ double oracle_compute_keff64(const oracle_problem *P, const double *fine_flux,
   }
   return fi / (ab + leakage);
 }
+
+/* ------------------------------------------------------------------------ */
+/* FP64 adjoint: reverse mode of attenuate64 over every track                */
+/* ------------------------------------------------------------------------ */
+typedef struct seg64 {
+  int64_t qrow, frow;   /* first fitted row and tally row (row index, not x G) */
+  int64_t srow;         /* sigma_t row */
+  double zin, ds;
+} seg64;
+
+static seg64 geometry64(const oracle_problem *P, float z, float ds_f, int64_t s)
+{
+  seg64 g;
+  const int F = P->F;
+  float dz_f = fine_dz(P);
+  int idx = (int)(z / dz_f);
+  int fine_id = idx % F;
+  double dz = dz_f;
+  g.zin = (double)z - dz * (idx + 0.5);
+  int r0 = fine_id;
+  if (P->axial_exp == 2) {
+    if (fine_id == 0) { g.zin -= dz; r0 = 0; }
+    else if (fine_id == F - 1) { g.zin += dz; r0 = fine_id - 2; }
+    else r0 = fine_id - 1;
+  }
+  g.qrow = s * F + r0;
+  g.frow = s * F + fine_id;
+  g.srow = P->src_sigt[s];
+  g.ds = ds_f;
+  return g;
+}
+
+void oracle_adjoint64(const oracle_problem *P, const double *fine_source,
+                      const double *psi_in, const double *dphi, double *dq,
+                      double *dsigt, double *dpsi_in)
+{
+  const int64_t G = P->G, S = P->S;
+  const int64_t PZ = (int64_t)P->P * P->Z;
+  const int64_t N3D = P->N2D * PZ;
+  const int64_t NR = P->NS * P->F;
+  const double dz = fine_dz(P);
+  const double rd1 = 1.0 / (2.0 * dz), rd2 = 1.0 / (2.0 * dz * dz);
+  float Hd = P->height / P->decomp_ax;
+  memset(dq, 0, sizeof(double) * (size_t)(NR * G));
+  double *hist = (double *)malloc(sizeof(double) * (size_t)((S + 1) * G));
+  seg64 *segs = (seg64 *)malloc(sizeof(seg64) * (size_t)S);
+  for (int64_t t = 0; t < N3D; t++) {
+    int64_t i = t / PZ;
+    int j = (int)((t / P->Z) % P->P);
+    float theta = P->polar_angles[j];
+    float mu_f = oracle_mu(theta);
+    const double mu = mu_f, mu2 = mu * mu;
+    const double w = (double)(P->p_weight[t] * P->az_weight[i]);
+    float z = P->z0[t];
+    for (int64_t g = 0; g < G; g++)
+      hist[g] = psi_in ? psi_in[t * G + g] : 0.0;
+    /* forward: psi entering every segment */
+    for (int64_t n = 0; n < S; n++) {
+      float ds = oracle_ds(P->seg_len[i * S + n], theta);
+      segs[n] = geometry64(P, z, ds, P->seg_src[t * S + n]);
+      const seg64 *sg = &segs[n];
+      for (int64_t g = 0; g < G; g++) {
+        const double sig = P->sigt[sg->srow * G + g], tau = sig * sg->ds;
+        const double e = -expm1(-tau), p = hist[n * G + g];
+        double pn;
+        if (P->axial_exp == 2) {
+          const double *qr = fine_source + sg->qrow * G;
+          const double y1 = qr[g], y2 = qr[G + g], y3 = qr[2 * G + g];
+          const double c1 = (y1 - y3) * rd1, c2 = (y1 - 2.0 * y2 + y3) * rd2;
+          const double q0 = y2 + c1 * sg->zin + c2 * sg->zin * sg->zin;
+          const double q1 = c1 + 2.0 * c2 * sg->zin, sig2 = sig * sig;
+          const double reuse = tau * (tau - 2.0) + 2.0 * e / (sig * sig2);
+          pn = q0 * e / sig + q1 * mu * (tau - e) / sig2 + c2 * mu2 * reuse + p * (1.0 - e);
+        } else {
+          pn = p - (p - fine_source[sg->qrow * G + g] / sig) * e;
+        }
+        hist[(n + 1) * G + g] = pn;
+      }
+      z = oracle_advance_z(z, ds, mu_f, Hd);
+    }
+    /* reverse */
+    for (int64_t g = 0; g < G; g++) {
+      double pbar = 0.0;
+      for (int64_t n = S - 1; n >= 0; n--) {
+        const seg64 *sg = &segs[n];
+        const double sig = P->sigt[sg->srow * G + g], ds = sg->ds, tau = sig * ds;
+        const double e = -expm1(-tau), eps = 1.0 - e, psi = hist[n * G + g];
+        const double r1 = 1.0 / sig, r2 = r1 * r1, r3 = r2 * r1;
+        const double lam = dphi[sg->frow * G + g];
+        if (P->axial_exp == 2) {
+          const double abar = lam * w;
+          const double r4 = r2 * r2 / 3.0;
+          const double *qr = fine_source + sg->qrow * G;
+          const double y1 = qr[g], y2 = qr[G + g], y3 = qr[2 * G + g];
+          const double zin = sg->zin;
+          const double c1 = (y1 - y3) * rd1, c2 = (y1 - 2.0 * y2 + y3) * rd2;
+          const double q0 = y2 + c1 * zin + c2 * zin * zin, q1 = c1 + 2.0 * c2 * zin, q2 = c2;
+          const double R = tau * (tau - 2.0) + 2.0 * e * r3;
+          const double Cc = tau * (tau * (tau - 3.0) + 6.0) - 6.0 * e;
+          const double tme = tau - e;
+          const double q0b = abar * tme * r2 + pbar * e * r1;
+          const double q1b = mu * (abar * R + pbar * tme * r2);
+          const double q2b = mu2 * (abar * Cc * r4 + pbar * R);
+          const double c1b = q0b * zin + q1b;
+          const double c2b = q0b * zin * zin + 2.0 * q1b * zin + q2b;
+          dq[sg->qrow * G + g] += c1b * rd1 + c2b * rd2;
+          dq[(sg->qrow + 1) * G + g] += q0b - 2.0 * c2b * rd2;
+          dq[(sg->qrow + 2) * G + g] += c2b * rd2 - c1b * rd1;
+          const double A = (q0 * tau + (sig * psi - q0) * e) * r2;
+          const double dA = (q0 * ds + psi * e + (sig * psi - q0) * eps * ds) * r2 - 2.0 * A * r1;
+          const double dR = (2.0 * tau - 2.0) * ds + 2.0 * eps * ds * r3 - 6.0 * e * r3 * r1;
+          const double dC = ((3.0 * tau - 6.0) * tau + 6.0) * ds - 6.0 * eps * ds;
+          const double dfi = dA + q1 * mu * dR + q2 * mu2 * (dC * r4 - 4.0 * Cc * r4 * r1);
+          const double dpn = q0 * (eps * ds * r1 - e * r2) + q1 * mu * (e * ds * r2 - 2.0 * tme * r3)
+                           + q2 * mu2 * dR - psi * eps * ds;
+          dsigt[sg->srow * G + g] += abar * dfi + pbar * dpn;
+          pbar = pbar * eps + abar * e * r1;
+        } else {
+          const double abar = lam * w * mu;
+          const double y = fine_source[sg->qrow * G + g];
+          const double dbar = abar - pbar;
+          dq[sg->qrow * G + g] += -dbar * e * r1;
+          dsigt[sg->srow * G + g] += dbar * (y * r2 * e + (psi - y * r1) * eps * ds);
+          pbar = pbar + dbar * e;
+        }
+      }
+      if (dpsi_in)
+        dpsi_in[t * G + g] = pbar;
+    }
+  }
+  free(hist);
+  free(segs);
+}

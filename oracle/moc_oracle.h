@@ -127,6 +127,14 @@ double oracle_update_sources64(const oracle_problem *P, const double *fine_flux,
 double oracle_compute_keff64(const oracle_problem *P, const double *fine_flux,
                              double leakage);
 
+/* FP64 adjoint of one sweep (oracle_sweep64's arithmetic): given dL/dphi,
+ * writes dL/dq [NS*F*G], adds dL/dsigma_t into dsigt [n_sigt*G], and writes
+ * dL/dpsi entering each track [N3D*G] (may be NULL).  psi_in is the angular
+ * flux entering the tracks (NULL = zero). */
+void oracle_adjoint64(const oracle_problem *P, const double *fine_source,
+                      const double *psi_in, const double *dphi, double *dq,
+                      double *dsigt, double *dpsi_in);
+
 #ifdef __cplusplus
 }
 #endif

@@ -99,6 +99,16 @@ SIGNATURES = {
     "moc_time_sweep": (C.c_int, [C.c_void_p, C.c_int, f64p]),
     "moc_launch_count": (C.c_int64, [C.c_void_p]),
     "moc_time_power_iterations": (C.c_int, [C.c_void_p, C.c_int, f64p, f64p, f64p, f64p]),
+    "moc_set_fine_source_device": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "moc_set_fine_source64_device": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "moc_set_sigma_t": (C.c_int, [C.c_void_p, f32p]),
+    "moc_zero_state": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "moc_get_fine_flux_device": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "moc_get_fine_flux64_device": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "moc_adjoint_forward": (C.c_int, [C.c_void_p, C.c_int]),
+    "moc_adjoint_backward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                       C.c_void_p]),
+    "moc_set_adjoint_width": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "moc_batch_create": (C.c_int, [C.c_int, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]),
     "moc_batch_destroy": (C.c_int, [C.c_void_p]),
     "moc_batch_autotune": (C.c_int, [C.c_void_p]),

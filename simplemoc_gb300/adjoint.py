@@ -1,0 +1,105 @@
+"""Differentiable transport sweep for PyTorch.
+
+`TransportSweep` is a torch.autograd.Function over the C ABI: its forward is
+one fixed-source sweep on the GPU (MIXED arithmetic, tallies from zero, psi
+checkpointed every k segments) and its backward is the hand-written reverse
+sweep (moc_adjoint_backward), which returns dL/d fine_source and dL/d sigma_t
+for whatever loss the caller builds on the scalar flux.
+
+`FixedSourceLoss` is the adjoint workload: the source is one update_sources
+step (src/solver.c:1235-1300) from a given scalar flux phi0,
+    q = (chi * (nuSigmaF . phi0) / k + S phi0) / (4 pi),
+written in torch so that the scatter matrices and nu*SigmaF enter the graph, and
+the loss is sum over fine regions of vol * nuSigmaF * phi after the sweep.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+
+import numpy as np
+import torch
+
+from . import _lib as L
+from .problem import HostProblem
+from .solver import Solver
+
+
+def _sync_torch(device: torch.device) -> None:
+    torch.cuda.current_stream(device).synchronize()
+
+
+class TransportSweep(torch.autograd.Function):
+    """phi = sweep(q, sigma_t); q [NS*F*G] float32 CUDA, sigma_t [n_sigt, G]."""
+
+    @staticmethod
+    def forward(ctx, q: torch.Tensor, sigma_t: torch.Tensor, solver: Solver, k_ckpt: int = 8):
+        lib = solver._lib
+        h = solver.handle
+        dev = q.device
+        qc = q.detach().contiguous()
+        sig = np.ascontiguousarray(sigma_t.detach().to("cpu", torch.float32).numpy().ravel())
+        _sync_torch(dev)
+        L.check(lib.moc_set_sigma_t(h, L.ptr(sig, C.c_float)), "moc_set_sigma_t")
+        L.check(lib.moc_set_fine_source_device(h, qc.data_ptr()), "moc_set_fine_source_device")
+        L.check(lib.moc_zero_state(h, 1, 1), "moc_zero_state")
+        L.check(lib.moc_adjoint_forward(h, k_ckpt), "moc_adjoint_forward")
+        phi = torch.empty_like(qc)
+        L.check(lib.moc_get_fine_flux_device(h, phi.data_ptr()), "moc_get_fine_flux_device")
+        solver.synchronize()
+        ctx.solver = solver
+        ctx.sig_shape = sigma_t.shape
+        ctx.sig_dtype = sigma_t.dtype
+        ctx.sig_device = sigma_t.device
+        return phi
+
+    @staticmethod
+    def backward(ctx, dphi: torch.Tensor):
+        solver = ctx.solver
+        lib = solver._lib
+        dphi = dphi.detach().to(torch.float32).contiguous()
+        dq = torch.empty_like(dphi)
+        dsig = torch.empty(int(np.prod(ctx.sig_shape)), dtype=torch.float64, device=dphi.device)
+        _sync_torch(dphi.device)
+        L.check(lib.moc_adjoint_backward(solver.handle, dphi.data_ptr(), dq.data_ptr(),
+                                         dsig.data_ptr(), None), "moc_adjoint_backward")
+        solver.synchronize()
+        return (dq, dsig.reshape(ctx.sig_shape).to(ctx.sig_device, ctx.sig_dtype), None, None)
+
+
+def sweep(q: torch.Tensor, sigma_t: torch.Tensor, solver: Solver, k_ckpt: int = 8) -> torch.Tensor:
+    return TransportSweep.apply(q, sigma_t, solver, k_ckpt)
+
+
+class FixedSourceLoss:
+    """Loss of the adjoint workload as a function of (sigma_t, S, nu*SigmaF, phi0)."""
+
+    def __init__(self, hp: HostProblem, solver: Solver, device: str = "cuda", keff: float = 1.0,
+                 k_ckpt: int = 8):
+        s = hp.spec
+        self.hp, self.solver, self.keff, self.k = hp, solver, keff, k_ckpt
+        self.G, self.F, self.NS = s.n_groups, s.fai, s.n_sources
+        n_xs = hp.xs.size // (3 * self.G)
+        self.dev = torch.device(device)
+        xs = torch.from_numpy(hp.xs.reshape(n_xs, self.G, 3).copy())
+        self.chi = xs[:, :, 2].to(self.dev)
+        self.src_xs = torch.from_numpy(hp.src_xs.astype(np.int64)).to(self.dev)
+        self.vol = torch.from_numpy(hp.vol.copy()).to(self.dev)
+
+    def source(self, phi0, scatter, nusf):
+        """update_sources from phi0 [NS, F, G] (src/solver.c:1266-1290)."""
+        Sm = scatter[self.src_xs]                      # [NS, G, G], row g = destination
+        nf = nusf[self.src_xs]                         # [NS, G]
+        fission = torch.einsum("sfg,sg->sf", phi0, nf) / self.keff
+        scat = torch.einsum("sgh,sfh->sfg", Sm, phi0)
+        return (fission[:, :, None] * self.chi[self.src_xs][:, None, :] + scat) / (4.0 * math.pi)
+
+    def loss_of_flux(self, phi, nusf):
+        """sum over fine regions of vol * nuSigmaF * phi."""
+        w = self.vol[:, None, None] * nusf[self.src_xs][:, None, :]
+        return (w * phi.reshape(self.NS, self.F, self.G)).sum()
+
+    def __call__(self, sigma_t, scatter, nusf, phi0):
+        q = self.source(phi0, scatter, nusf).reshape(-1).to(torch.float32)
+        phi = sweep(q, sigma_t, self.solver, self.k)
+        return self.loss_of_flux(phi.to(nusf.dtype), nusf), q

@@ -3,6 +3,7 @@
 // src/solver.c (transport_sweep, renormalize_flux, update_sources,
 // compute_keff) over device-resident storage.
 #include <cuda_runtime.h>
+#include <math.h>
 #include <stdint.h>
 #include <string.h>
 
@@ -183,6 +184,7 @@ void release(moc_problem *p) {
   dfree(p->psi_f); dfree(p->psi_b); dfree(p->q64); dfree(p->phi64); dfree(p->psi_f64);
   dfree(p->psi_b64); dfree(p->partials); dfree(p->scalars); dfree(p->err);
   dfree(p->xs_order); dfree(p->upd_items); dfree(p->psi_scale); dfree(p->psi_b_nonzero);
+  dfree(p->ck_psi); dfree(p->ck_z); dfree(p->adj_dphi); dfree(p->adj_dq); dfree(p->adj_dsig);
   if (p->ev0) cudaEventDestroy(p->ev0);
   if (p->ev1) cudaEventDestroy(p->ev1);
   if (p->stream) cudaStreamDestroy(p->stream);
@@ -436,6 +438,20 @@ int moc_set_launch(moc_problem *p, int threads_per_track, int chunks_per_thread)
   return MOC_ERR_UNSUPPORTED;
 }
 
+int moc_set_adjoint_width(moc_problem *p, int lanes_per_track, int chunks_per_lane) {
+  if (!p) return MOC_ERR_ARG;
+  if (lanes_per_track == 0 && chunks_per_lane == 0) {
+    p->adj_tpw = p->adj_cpl = 0;
+    return MOC_OK;
+  }
+  if (lanes_per_track < 1 || lanes_per_track > 32 || chunks_per_lane < 1 || chunks_per_lane > 2)
+    return MOC_ERR_UNSUPPORTED;
+  if ((int64_t)lanes_per_track * chunks_per_lane * 4 < p->ldg) return MOC_ERR_ARG;
+  p->adj_tpw = lanes_per_track;
+  p->adj_cpl = chunks_per_lane;
+  return MOC_OK;
+}
+
 int moc_get_launch(const moc_problem *p, int *threads_per_track, int *chunks_per_thread) {
   if (!p || !threads_per_track || !chunks_per_thread) return MOC_ERR_ARG;
   return moc_sweep_launch_shape(p, threads_per_track, chunks_per_thread);
@@ -593,6 +609,162 @@ int moc_time_power_iterations(moc_problem *p, int iters, double *ms_total, doubl
   if (rc != MOC_OK) return rc;
   if (keff) *keff = sc[SC_KEFF];
   if (residual) *residual = sc[SC_RESIDUAL];
+  return MOC_OK;
+}
+
+}  // extern "C"
+
+// ---- state access on device pointers (the torch binding) -----------------
+namespace {
+template <typename T>
+int copy_rows_dd(moc_problem *p, T *dst, int64_t dpitch, const T *src, int64_t spitch,
+                 int64_t rows, int64_t width) {
+  MOC_CUDA_TRY(cudaMemcpy2DAsync(dst, sizeof(T) * dpitch, src, sizeof(T) * spitch,
+                                 sizeof(T) * width, (size_t)rows, cudaMemcpyDeviceToDevice,
+                                 p->stream));
+  return MOC_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int moc_set_fine_source_device(moc_problem *p, const float *q) {
+  int rc = usable(p);
+  if (rc != MOC_OK) return rc;
+  if (!q) return MOC_ERR_ARG;
+  cudaSetDevice(p->device);
+  const int64_t G = p->d.n_groups;
+  rc = copy_rows_dd(p, p->q, p->ldg, q, G, p->nfsr, G);
+  if (rc == MOC_OK && p->q64) {
+    widen_kernel<<<1024, 256, 0, p->stream>>>(p->q, p->q64, p->nfsr * p->ldg);
+    p->launches++;
+  }
+  return rc == MOC_OK ? MOC_OK : fail(p, rc);
+}
+
+int moc_set_fine_source64_device(moc_problem *p, const double *q) {
+  int rc = usable(p);
+  if (rc != MOC_OK) return rc;
+  if (!q || !p->q64) return !q ? MOC_ERR_ARG : MOC_ERR_STATE;
+  cudaSetDevice(p->device);
+  rc = copy_rows_dd(p, p->q64, p->ldg, q, (int64_t)p->d.n_groups, p->nfsr, p->d.n_groups);
+  return rc == MOC_OK ? MOC_OK : fail(p, rc);
+}
+
+int moc_set_sigma_t(moc_problem *p, const float *sigt) {
+  int rc = usable(p);
+  if (rc != MOC_OK) return rc;
+  if (!sigt) return MOC_ERR_ARG;
+  for (int64_t k = 0; k < (int64_t)p->d.n_sigt * p->d.n_groups; ++k)
+    if (!(sigt[k] > 0.0f) || isinf(sigt[k])) return MOC_ERR_ARG;
+  cudaSetDevice(p->device);
+  std::vector<float> coef((size_t)p->d.n_sigt * COEF_PLANES * p->ldg);
+  moc_host_coef(&p->d, sigt, p->ldg, coef.data());
+  rc = put(p, p->coef, coef.data(), (int64_t)coef.size());
+  if (rc == MOC_OK && cudaStreamSynchronize(p->stream) != cudaSuccess) rc = MOC_ERR_CUDA;
+  return rc == MOC_OK ? MOC_OK : fail(p, rc);
+}
+
+int moc_zero_state(moc_problem *p, int flux, int psi) {
+  int rc = usable(p);
+  if (rc != MOC_OK) return rc;
+  cudaSetDevice(p->device);
+  const size_t fb = sizeof(float) * (size_t)(p->nfsr * p->ldg);
+  const size_t pb = sizeof(float) * (size_t)(p->n3d * p->ldg);
+  if (flux) {
+    MOC_CUDA_TRY(cudaMemsetAsync(p->phi, 0, fb, p->stream));
+    if (p->phi_lo) MOC_CUDA_TRY(cudaMemsetAsync(p->phi_lo, 0, fb, p->stream));
+    if (p->phi64) MOC_CUDA_TRY(cudaMemsetAsync(p->phi64, 0, 2 * fb, p->stream));
+  }
+  if (psi) {
+    MOC_CUDA_TRY(cudaMemsetAsync(p->psi_f, 0, pb, p->stream));
+    MOC_CUDA_TRY(cudaMemsetAsync(p->psi_b, 0, pb, p->stream));
+    if (p->psi_f64) MOC_CUDA_TRY(cudaMemsetAsync(p->psi_f64, 0, 2 * pb, p->stream));
+    if (p->psi_b64) MOC_CUDA_TRY(cudaMemsetAsync(p->psi_b64, 0, 2 * pb, p->stream));
+    if (p->psi_pending) {
+      p->psi_pending = false;
+      rc = moc_reset_psi_scale(p);
+      if (rc != MOC_OK) return fail(p, rc);
+    }
+    rc = moc_detect_psi_b(p);
+    if (rc != MOC_OK) return fail(p, rc);
+  }
+  return MOC_OK;
+}
+
+int moc_get_fine_flux_device(moc_problem *p, float *phi) {
+  int rc = usable(p);
+  if (rc != MOC_OK) return rc;
+  if (!phi) return MOC_ERR_ARG;
+  cudaSetDevice(p->device);
+  rc = copy_rows_dd(p, phi, (int64_t)p->d.n_groups, p->phi, p->ldg, p->nfsr, p->d.n_groups);
+  return rc == MOC_OK ? MOC_OK : fail(p, rc);
+}
+
+int moc_get_fine_flux64_device(moc_problem *p, double *phi) {
+  int rc = usable(p);
+  if (rc != MOC_OK) return rc;
+  if (!phi || !p->phi64) return !phi ? MOC_ERR_ARG : MOC_ERR_STATE;
+  cudaSetDevice(p->device);
+  rc = copy_rows_dd(p, phi, (int64_t)p->d.n_groups, p->phi64, p->ldg, p->nfsr, p->d.n_groups);
+  return rc == MOC_OK ? MOC_OK : fail(p, rc);
+}
+
+// ---- adjoint ---------------------------------------------------------------
+
+int moc_adjoint_forward(moc_problem *p, int k_ckpt) {
+  int rc = usable(p);
+  if (rc != MOC_OK) return rc;
+  if (k_ckpt < 1 || k_ckpt > 8) return MOC_ERR_ARG;
+  if (p->d.n_groups > 256) return MOC_ERR_UNSUPPORTED;
+  cudaSetDevice(p->device);
+  const int nck = (p->d.n_seg + k_ckpt - 1) / k_ckpt;
+  if (!p->ck_psi || p->ck_n != nck) {
+    dfree(p->ck_psi);
+    dfree(p->ck_z);
+    rc = dalloc(p, &p->ck_psi, p->n3d * nck * p->ldg);
+    if (rc == MOC_OK) rc = dalloc(p, &p->ck_z, p->n3d * nck);
+    if (rc != MOC_OK) return rc;
+  }
+  p->ck_k = k_ckpt;
+  p->ck_n = nck;
+  const bool had_pending = p->psi_pending;
+  rc = moc_launch_sweep_ckpt(p, p->ck_psi, p->ck_z, k_ckpt, nck);
+  if (rc != MOC_OK) return fail(p, rc);
+  if (had_pending) {
+    p->psi_pending = false;
+    rc = moc_reset_psi_scale(p);
+    if (rc != MOC_OK) return fail(p, rc);
+  }
+  return MOC_OK;
+}
+
+int moc_adjoint_backward(moc_problem *p, const float *dphi, float *dq, double *dsigt,
+                         float *dpsi_in) {
+  int rc = usable(p);
+  if (rc != MOC_OK) return rc;
+  if (!dphi || !p->ck_psi) return !dphi ? MOC_ERR_ARG : MOC_ERR_STATE;
+  cudaSetDevice(p->device);
+  const int64_t G = p->d.n_groups;
+  if (!p->adj_dphi) {
+    rc = dalloc(p, &p->adj_dphi, p->nfsr * p->ldg);
+    if (rc == MOC_OK) rc = dalloc(p, &p->adj_dq, p->nfsr * p->ldg);
+    if (rc == MOC_OK) rc = dalloc(p, &p->adj_dsig, (int64_t)p->d.n_sigt * p->ldg);
+    if (rc != MOC_OK) return rc;
+  }
+  const size_t fb = sizeof(float) * (size_t)(p->nfsr * p->ldg);
+  MOC_CUDA_TRY(cudaMemsetAsync(p->adj_dphi, 0, fb, p->stream));
+  MOC_CUDA_TRY(cudaMemsetAsync(p->adj_dq, 0, fb, p->stream));
+  MOC_CUDA_TRY(cudaMemsetAsync(p->adj_dsig, 0, sizeof(double) * (size_t)p->d.n_sigt * p->ldg,
+                               p->stream));
+  rc = copy_rows_dd(p, p->adj_dphi, p->ldg, dphi, G, p->nfsr, G);
+  if (rc == MOC_OK)
+    rc = moc_launch_adjoint(p, p->ck_psi, p->ck_z, p->ck_k, p->ck_n, p->adj_dphi, p->adj_dq,
+                            p->adj_dsig, dpsi_in);
+  if (rc == MOC_OK && dq) rc = copy_rows_dd(p, dq, G, p->adj_dq, p->ldg, p->nfsr, G);
+  if (rc == MOC_OK && dsigt)
+    rc = copy_rows_dd(p, dsigt, G, p->adj_dsig, p->ldg, (int64_t)p->d.n_sigt, G);
+  if (rc != MOC_OK) return fail(p, rc);
   return MOC_OK;
 }
 

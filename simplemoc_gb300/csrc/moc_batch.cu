@@ -49,10 +49,14 @@ struct WidthKey {
 std::mutex g_width_mu;
 std::map<WidthKey, int> g_width_cache;
 
+// Two 4-group chunks per thread (the batched kernel's shape): the narrowest
+// power-of-two width that covers the groups.
+constexpr int BATCH_CPL = 2;
+
 int default_width(const moc_problem *p) {
   const int nchunk = p->ldg / 4;
   int w = 4;
-  while (w < nchunk) w <<= 1;
+  while (w * BATCH_CPL < nchunk) w <<= 1;
   return w;
 }
 
@@ -145,7 +149,7 @@ int moc_batch_create(int n, moc_problem *const *problems, moc_batch **out) {
   for (moc_problem *p : b->cores) {
     // one launch: same device, mode, source order and (PLAIN) exponential table
     if (!p || p->status != MOC_OK || p->device != b->device || p->mode != b->mode ||
-        (p->d.axial_exp == 2) != b->quad || p->ldg > 128 || p->mode == MOC_MODE_FP64 ||
+        (p->d.axial_exp == 2) != b->quad || p->ldg > 256 || p->mode == MOC_MODE_FP64 ||
         (p->mode == MOC_MODE_MIXED && (p->flags & MOC_FLAG_COMPENSATED)) ||
         p->d.table_n != p0->d.table_n || p->d.table_dx != p0->d.table_dx ||
         p->d.table_maxval != p0->d.table_maxval) {
@@ -197,7 +201,7 @@ int moc_batch_set_width(moc_batch *b, int core, int threads_per_track) {
   if (!b || core < 0 || core >= (int)b->cores.size()) return MOC_ERR_ARG;
   const int w = threads_per_track;
   if (w != 4 && w != 8 && w != 16 && w != 32) return MOC_ERR_ARG;
-  if (w * 4 < b->cores[(size_t)core]->ldg) return MOC_ERR_ARG;
+  if (w * 4 * BATCH_CPL < b->cores[(size_t)core]->ldg) return MOC_ERR_ARG;
   b->tpw[(size_t)core] = w;
   cudaSetDevice(b->device);
   return rebuild_tasks(b);
@@ -258,7 +262,7 @@ int moc_batch_autotune(moc_batch *b) {
     double best = 1e30;
     int bw = default_width(p);
     for (int w = 4; w <= 32 && rc == MOC_OK; w <<= 1) {
-      if (w * 4 < p->ldg) continue;
+      if (w * 4 * BATCH_CPL < p->ldg) continue;
       const int gpw = 32 / w;
       std::vector<int2> t;
       for (int64_t k = 0; k < nsub; k += gpw) t.push_back(make_int2(0, (int)k));

@@ -210,10 +210,20 @@ int moc_host_derive(const moc_dims *d, const moc_host *h, int32_t ldg, float *se
     const int64_t i = t / (P * Z);
     weight[t] = h->p_weight[t] * h->az_weight[i];                          // src/solver.c:49
   }
+  moc_host_coef(d, h->sigt, ldg, coef);
+  for (int64_t m = 0; m < d->n_xs; m++)
+    for (int64_t g = 0; g < G; g++)
+      for (int64_t g2 = 0; g2 < G; g2++)
+        scatter_t[(m * G + g2) * G + g] = h->scatter[(m * G + g) * G + g2];
+  return MOC_OK;
+}
+
+void moc_host_coef(const moc_dims *d, const float *sigt, int32_t ldg, float *coef) {
+  const int64_t G = d->n_groups;
   for (int64_t m = 0; m < d->n_sigt; m++) {
     float *c = coef + m * 8 * (int64_t)ldg;
     for (int64_t g = 0; g < ldg; g++) {
-      const float sig = g < G ? h->sigt[m * G + g] : 1.0f;
+      const float sig = g < G ? sigt[m * G + g] : 1.0f;
       const float sig2 = sig * sig;                                        // src/solver.c:153
       const float sig3 = sig * sig2;                                       // src/solver.c:176
       const float sig4 = 3.f * sig2 * sig2;                                // src/solver.c:198
@@ -227,11 +237,6 @@ int moc_host_derive(const moc_dims *d, const moc_host *h, int32_t ldg, float *se
       c[7 * ldg + g] = 1.0f / sig4;
     }
   }
-  for (int64_t m = 0; m < d->n_xs; m++)
-    for (int64_t g = 0; g < G; g++)
-      for (int64_t g2 = 0; g2 < G; g2++)
-        scatter_t[(m * G + g2) * G + g] = h->scatter[(m * G + g) * G + g2];
-  return MOC_OK;
 }
 
 int moc_host_validate(const moc_dims *d, const moc_host *h) {

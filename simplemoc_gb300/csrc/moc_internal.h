@@ -43,6 +43,11 @@ struct SweepArgs {
   float hd;                 // domain height
   uint32_t fmagic;          // zi % F == zi - F*umulhi(zi, fmagic) for reachable zi; 0 = use %
   int32_t *err;             // device error word (0 = ok)
+  // psi checkpoints of the adjoint's forward sweep: every ck_k segments,
+  // ck_n per track ([N3D][ck_n][ldg] and [N3D][ck_n] heights)
+  float *ck_psi;
+  float *ck_z;
+  int32_t ck_k, ck_n;
   // variable-length sub-segment streams (reference traversal), else null
   const int64_t *csr_off;   // [N3D+1]
   const float *csr_ds;      // [M] sub-segment lengths
@@ -58,6 +63,7 @@ struct moc_problem {
   int mode = MOC_MODE_PLAIN;
   int flags = 0;
   int tpw = 0, cpl = 0;          // 0 = automatic
+  int adj_tpw = 0, adj_cpl = 0;  // reverse sweep lanes per track, chunks per lane; 0 = automatic
   int64_t launches = 0;
   int64_t n3d = 0, nfsr = 0;
   int32_t ldg = 0;
@@ -84,6 +90,11 @@ struct moc_problem {
   float *psi_scale = nullptr;
   int32_t *psi_b_nonzero = nullptr;
   bool psi_pending = false;
+  // adjoint: psi checkpoints of the last moc_adjoint_forward and work arrays
+  float *ck_psi = nullptr, *ck_z = nullptr;
+  int32_t ck_k = 0, ck_n = 0;
+  float *adj_dphi = nullptr, *adj_dq = nullptr;
+  double *adj_dsig = nullptr;
   // reductions / scalars
   double *partials = nullptr;    // [3 * RED_BLOCKS]
   double *scalars = nullptr;     // see post kernels
@@ -103,6 +114,9 @@ int moc_launch_sweep_batch(int device, cudaStream_t st, int mode, bool quad, con
                            const int2 *tasks, int64_t n_tasks, const int *tpw,
                            unsigned long long *counter, const float2 *table, int table_n);
 int moc_reset_psi_scale(moc_problem *p);
+int moc_launch_sweep_ckpt(moc_problem *p, float *ck_psi, float *ck_z, int k, int nck);
+int moc_launch_adjoint(moc_problem *p, const float *ck_psi, const float *ck_z, int k, int nck,
+                       const float *dphi, float *dq, double *dsig, float *dpsi_in);
 int moc_sweep_launch_shape(const moc_problem *p, int *tpw, int *cpl);
 int moc_sweep_autotune(moc_problem *p, int64_t n_sub, int *tpw, int *cpl, double *ms);
 int moc_launch_renormalize(moc_problem *p);

@@ -95,6 +95,7 @@ __device__ __forceinline__ float one_minus_exp(float t) {
 
 struct Seg {
   float zin;      // height within the fitted interval (after edge shift)
+  int mat;        // sigma_t row of the source region
   int64_t qrow;   // first of the three fine-source rows (quadratic) or the row (flat)
   int64_t frow;   // tally row
   int64_t crow;   // coefficient block
@@ -123,7 +124,8 @@ __device__ __forceinline__ Seg segment_geometry(const SweepArgs &a, float z, int
   int64_t base = (int64_t)s * a.F;
   g.qrow = (base + r0) * a.ldg;
   g.frow = (base + fine) * a.ldg;
-  g.crow = (int64_t)__ldg(a.src_sigt + s) * COEF_PLANES * a.ldg;
+  g.mat = __ldg(a.src_sigt + s);
+  g.crow = (int64_t)g.mat * COEF_PLANES * a.ldg;
   return g;
 }
 
@@ -259,7 +261,7 @@ __device__ __forceinline__ int checked_source(const SweepArgs &a, int s, int li)
 // One 3D track (or one group of TPW lanes' track) of the sweep.  TPW_CT is
 // the threads per track when known at compile time; 0 takes tpw_rt (the
 // batched kernel, where each core has its own width).
-template <int TPW_CT, int CPL, int MODE, bool QUAD, bool CSR>
+template <int TPW_CT, int CPL, int MODE, bool QUAD, bool CSR, bool CKPT = false>
 __device__ __forceinline__ void sweep_track(const SweepArgs &a, int64_t track, int lane,
                                             int tpw_rt, const float2 *s_table) {
   const int TPW = TPW_CT ? TPW_CT : tpw_rt;
@@ -324,7 +326,24 @@ __device__ __forceinline__ void sweep_track(const SweepArgs &a, int64_t track, i
   Rows<CPL, QUAD> rows;
   if (S > 0) load_rows<CPL, QUAD>(a, g, li, TPW, rows);
 
+  int ck_left = 0;                       // segments to the next checkpoint
+  int64_t ck_slot = CKPT ? tr * a.ck_n : 0;
   for (int n = 0; n < S; ++n) {
+    if (CKPT && ck_left-- == 0) {
+      // angular flux and height entering segment n (n a multiple of ck_k),
+      // for the reverse sweep
+      ck_left = a.ck_k - 1;
+      if (valid) {
+#pragma unroll
+        for (int k = 0; k < CPL; ++k) {
+          const int c = li + TPW * k;
+          if (c < a.nchunk)
+            *reinterpret_cast<float4 *>(a.ck_psi + ck_slot * a.ldg + 4 * c) = psi[k];
+        }
+        if (li == 0) a.ck_z[ck_slot] = z;
+      }
+      ++ck_slot;
+    }
     float z_next = CSR ? 0.f : advance_z(a, z, ds, mu);
     // ---- issue the loads of segment n+1 before the arithmetic of segment n
     float ds1 = 0.f;
@@ -431,7 +450,7 @@ __device__ __forceinline__ void sweep_track(const SweepArgs &a, int64_t track, i
   }
 }
 
-template <int TPW, int CPL, int MODE, bool QUAD, bool CSR = false>
+template <int TPW, int CPL, int MODE, bool QUAD, bool CSR = false, bool CKPT = false>
 __global__ void __launch_bounds__(BLOCK) sweep_kernel(SweepArgs a) {
   extern __shared__ float2 s_table[];
   if (MODE == MODE_PLAIN) {
@@ -445,8 +464,12 @@ __global__ void __launch_bounds__(BLOCK) sweep_kernel(SweepArgs a) {
   const int64_t n_warps = ((int64_t)gridDim.x * BLOCK) >> 5;
   static_assert(!CSR || TPW == 32, "variable-length streams run one track per warp");
   for (int64_t base = warp_id * GPW; base < a.n3d; base += n_warps * GPW)
-    sweep_track<TPW, CPL, MODE, QUAD, CSR>(a, base + gw, lane, TPW, s_table);
+    sweep_track<TPW, CPL, MODE, QUAD, CSR, CKPT>(a, base + gw, lane, TPW, s_table);
 }
+
+// Chunks of 4 groups per thread in the batched kernel: with threads per track
+// from 4 to 32 this covers 8 to 256 groups.
+constexpr int BATCH_CPL = 2;
 
 // Batched sweep of many independent problems ("cores") in one persistent
 // launch.  Work = tasks (core, first track) of 32/tpw tracks each, ordered by
@@ -454,7 +477,7 @@ __global__ void __launch_bounds__(BLOCK) sweep_kernel(SweepArgs a) {
 // left (a work queue, not a wait).  Each core runs with its own threads per
 // track (tpw), so small group counts pack several tracks into a warp.
 template <int MODE, bool QUAD>
-__global__ void __launch_bounds__(BLOCK) sweep_batch_kernel(const SweepArgs *__restrict__ cores,
+__global__ void __launch_bounds__(BLOCK, 2) sweep_batch_kernel(const SweepArgs *__restrict__ cores,
                                                             const int2 *__restrict__ tasks,
                                                             int64_t n_tasks,
                                                             const int *__restrict__ core_tpw,
@@ -473,9 +496,10 @@ __global__ void __launch_bounds__(BLOCK) sweep_batch_kernel(const SweepArgs *__r
     t = __shfl_sync(FULL, t, 0);
     if (t >= (unsigned long long)n_tasks) break;
     const int2 task = tasks[t];
-    const SweepArgs &a = cores[task.x];
+    const SweepArgs a = cores[task.x];        // by value: the fields live in registers
     const int tpw = core_tpw[task.x];
-    sweep_track<0, 1, MODE, QUAD, false>(a, (int64_t)task.y + lane / tpw, lane, tpw, s_table);
+    sweep_track<0, BATCH_CPL, MODE, QUAD, false>(a, (int64_t)task.y + lane / tpw, lane, tpw,
+                                                 s_table);
   }
 }
 
@@ -557,9 +581,9 @@ __global__ void __launch_bounds__(BLOCK) sweep64_kernel(SweepArgs a) {
   }
 }
 
-template <int TPW, int CPL, int MODE, bool QUAD, bool CSR = false>
+template <int TPW, int CPL, int MODE, bool QUAD, bool CSR = false, bool CKPT = false>
 int launch_t(moc_problem *p, const SweepArgs &a) {
-  auto kern = sweep_kernel<TPW, CPL, MODE, QUAD, CSR>;
+  auto kern = sweep_kernel<TPW, CPL, MODE, QUAD, CSR, CKPT>;
   size_t smem = (MODE == MODE_PLAIN) ? sizeof(float2) * (size_t)a.table_n : 0;
   if (smem > 48 * 1024) {
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
@@ -856,3 +880,387 @@ int moc_launch_sweep_batch(int device, cudaStream_t st, int mode, bool quad, con
 }
 
 SweepArgs moc_sweep_args(moc_problem *p) { return build_args(p); }
+
+// ===========================================================================
+// Adjoint (reverse-mode) sweep of the MIXED arithmetic.
+//
+// The loss is any function of the scalar fluxes; the caller gives its gradient
+// dL/dphi.  Each segment adds tally = w * fi(psi, q, sigma) to one fine region
+// and maps psi to pn(psi, q, sigma) (per group, groups independent), so per
+// track and group the reverse sweep is a scalar recurrence
+//     psibar_n = psibar_{n+1} * dpn/dpsi + (w dL/dphi) * dfi/dpsi,
+// with the parameter adjoints accumulated from the same two partials.  psi_n
+// is recomputed forward from the checkpoint that the forward sweep stored
+// every ck_k (<= 8) segments, held in registers for the block, and consumed
+// backwards.  dL/dq goes to the three fine-source rows of every segment with
+// vector reductions; dL/dsigma_t is summed per sub-warp in shared memory and
+// added to an FP64 array once per block.
+// ===========================================================================
+namespace {
+
+constexpr int ADJ_KMAX = 8;
+
+struct AdjArgs {
+  SweepArgs a;
+  const float *dphi;      // [NS*F*ldg] dL/dphi
+  float *dq;              // [NS*F*ldg] dL/dq, added to
+  double *dsig;           // [n_sigt*ldg] dL/dsigma_t, added to
+  float *dpsi_in;         // [N3D*G] dL/dpsi entering each track, or null
+  int n_sigt;
+  int slices;             // 1: shared-memory accumulators per sub-warp
+  int tpw;                // lanes per track (any width 1..32)
+  int nsub;               // tracks per block: (BLOCK / 32) * (32 / tpw)
+};
+
+struct AdjOut {
+  float pbar, y1b, y2b, y3b, sbar;
+};
+
+__device__ __forceinline__ AdjOut adj_quad(const SweepArgs &a, float y1, float y2, float y3,
+                                           float sig, float r1, float zin, float ds, float mu,
+                                           float mu2, float psi, float pbar, float abar) {
+  const float r2 = r1 * r1, r3 = r1 * r2, r4 = r2 * r2 * (1.0f / 3.0f);
+  const float c1 = (y1 - y3) * a.rd1;
+  const float c2 = (fmaf(-2.f, y2, y1) + y3) * a.rd2;
+  const float q0 = fmaf(fmaf(c2, zin, c1), zin, y2);
+  const float q1 = fmaf(2.f * c2, zin, c1);
+  const float q2 = c2;
+  const float tau = sig * ds;
+  const float e = one_minus_exp(tau);
+  const float eps = 1.f - e;                          // exp(-tau)
+  const float R = fmaf(tau, tau - 2.f, 2.f * e * r3); // the reference's reuse term
+  const float Cc = fmaf(tau, fmaf(tau, tau - 3.f, 6.f), -6.f * e);
+  const float tme = tau - e;
+  AdjOut o;
+  o.pbar = pbar * eps + abar * e * r1;
+  const float q0b = abar * tme * r2 + pbar * e * r1;
+  const float q1b = mu * (abar * R + pbar * tme * r2);
+  const float q2b = mu2 * (abar * Cc * r4 + pbar * R);
+  const float c1b = fmaf(q0b, zin, q1b);
+  const float c2b = fmaf(fmaf(q0b, zin, 2.f * q1b), zin, q2b);
+  o.y1b = c1b * a.rd1 + c2b * a.rd2;
+  o.y2b = q0b - 2.f * c2b * a.rd2;
+  o.y3b = c2b * a.rd2 - c1b * a.rd1;
+  const float A = (q0 * tau + (sig * psi - q0) * e) * r2;
+  const float dA = (q0 * ds + psi * e + (sig * psi - q0) * eps * ds) * r2 - 2.f * A * r1;
+  const float dR = (2.f * tau - 2.f) * ds + 2.f * eps * ds * r3 - 6.f * e * r3 * r1;
+  const float dC = ((3.f * tau - 6.f) * tau + 6.f) * ds - 6.f * eps * ds;
+  const float dfi = dA + q1 * mu * dR + q2 * mu2 * (dC * r4 - 4.f * Cc * r4 * r1);
+  const float dpn = q0 * (eps * ds * r1 - e * r2) + q1 * mu * (e * ds * r2 - 2.f * tme * r3) +
+                    q2 * mu2 * dR - psi * eps * ds;
+  o.sbar = abar * dfi + pbar * dpn;
+  return o;
+}
+
+__device__ __forceinline__ AdjOut adj_flat(float y, float sig, float r1, float ds, float psi,
+                                           float pbar, float abar) {
+  const float e = one_minus_exp(sig * ds);
+  const float eps = 1.f - e;
+  const float dbar = abar - pbar;                     // dL/d(delta psi)
+  AdjOut o;
+  o.pbar = pbar + dbar * e;
+  o.y1b = -dbar * e * r1;
+  o.y2b = o.y3b = 0.f;
+  o.sbar = dbar * (y * r1 * r1 * e + (psi - y * r1) * eps * ds);
+  return o;
+}
+
+// The per-segment operands of one thread's chunks: sigma_t and 1/sigma_t, the
+// source rows and (reverse pass) dL/dphi of the tally row.
+template <int CPL, bool QUAD>
+struct AdjRows {
+  float4 sig[CPL], r1[CPL], y[CPL][QUAD ? 3 : 1], lam[CPL];
+};
+
+template <int CPL, bool QUAD, bool LAM>
+__device__ __forceinline__ void adj_load(const SweepArgs &a, const AdjArgs &x, const Seg &g,
+                                         int li, int TPW, AdjRows<CPL, QUAD> &r) {
+#pragma unroll
+  for (int k = 0; k < CPL; ++k) {
+    const int c = li + TPW * k;
+    if (c >= a.nchunk) continue;
+    const float *cf = a.coef + g.crow + 4 * c;
+    r.sig[k] = __ldg(reinterpret_cast<const float4 *>(cf));
+    r.r1[k] = __ldg(reinterpret_cast<const float4 *>(cf + 4 * a.ldg));
+const float *qr = a.q + g.qrow + 4 * c;
+    r.y[k][0] = ld_stream(qr);
+    if (QUAD) {
+      r.y[k][QUAD ? 1 : 0] = ld_stream(qr + a.ldg);
+      r.y[k][QUAD ? 2 : 0] = ld_stream(qr + 2 * a.ldg);
+    }
+    if (LAM) r.lam[k] = __ldg(reinterpret_cast<const float4 *>(x.dphi + g.frow + 4 * c));
+  }
+}
+
+// Shared memory of the reverse sweep: the recomputed angular flux of the
+// current checkpoint block (ADJ_KMAX x CPL float4 per thread), then the
+// per-sub-warp dL/dsigma_t accumulators when they fit.
+template <int CPL>
+constexpr size_t adj_hist_bytes() {
+  return sizeof(float4) * (size_t)BLOCK * ADJ_KMAX * CPL;
+}
+
+// Lanes per track are a runtime width: the kernel has no shuffles, so a track
+// of nchunk float4 chunks takes exactly ceil(nchunk / CPL) lanes and a warp
+// holds floor(32 / width) tracks (G = 40: 10 lanes, three tracks a warp).  The
+// lanes left over run the loops with no chunk so that the warp stays converged.
+template <int CPL, bool QUAD>
+__global__ void __launch_bounds__(BLOCK, 2) adjoint_kernel(AdjArgs x) {
+  extern __shared__ float4 s_adj[];
+  const SweepArgs &a = x.a;
+  const int TPW = x.tpw;
+  const int GPW = 32 / TPW;
+  const int lane = threadIdx.x & 31;
+  const bool idle = lane >= GPW * TPW;
+  const int li = idle ? (1 << 20) : lane % TPW;    // idle lanes own no chunk
+  const int gw = idle ? 0 : lane / TPW;
+  const int sub = (threadIdx.x >> 5) * GPW + gw;
+  // this thread's history slots: hist(jj, k) at s_adj[(jj * CPL + k) * BLOCK + threadIdx.x]
+  float4 *hist_base = s_adj + threadIdx.x;
+  // the block's segment geometry and lengths, one copy per track (written by
+  // its lane 0)
+  Seg *s_geo_all = reinterpret_cast<Seg *>(s_adj + (size_t)BLOCK * ADJ_KMAX * CPL);
+  Seg *s_geo = s_geo_all + (size_t)sub * ADJ_KMAX;
+  float *s_ds_all = reinterpret_cast<float *>(s_geo_all + (size_t)x.nsub * ADJ_KMAX);
+  float *s_ds = s_ds_all + (size_t)sub * ADJ_KMAX;
+  float *s_acc = s_ds_all + (size_t)x.nsub * ADJ_KMAX;
+  const int64_t per_slice = (int64_t)x.n_sigt * a.ldg;
+  float *acc = x.slices ? s_acc + sub * per_slice : nullptr;
+  if (x.slices) {
+    for (int64_t i = threadIdx.x; i < per_slice * x.nsub; i += BLOCK) s_acc[i] = 0.f;
+    __syncthreads();
+  }
+  const int64_t warp_id = ((int64_t)blockIdx.x * BLOCK + threadIdx.x) >> 5;
+  const int64_t n_warps = ((int64_t)gridDim.x * BLOCK) >> 5;
+  const int64_t PZ = (int64_t)a.P * a.Z;
+  const int S = a.S, K = a.ck_k, NCK = a.ck_n;
+  for (int64_t base = warp_id * GPW; base < a.n3d; base += n_warps * GPW) {
+    const int64_t track = base + gw;
+    const bool valid = !idle && track < a.n3d;
+    const int64_t tr = track < a.n3d ? track : a.n3d - 1;
+    const int64_t i2 = tr / PZ;
+    const int j = (int)((tr / a.Z) % a.P);
+    const float mu = a.mu[j];
+    const float mu2 = mu * mu;
+    const float w = a.weight[tr];
+    const float w_mu = w * mu;
+    const float *dsb = a.seg_ds + (i2 * a.P + j) * S;
+    const int32_t *srcb = a.seg_src + tr * S;
+    float4 pbar[CPL];
+#pragma unroll
+    for (int k = 0; k < CPL; ++k) pbar[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int b = NCK - 1; b >= 0; --b) {
+      const int n0 = b * K;
+      const int cnt = min(K, S - n0);
+      float4 psi[CPL];
+#pragma unroll
+      for (int k = 0; k < CPL; ++k) {
+        const int c = li + TPW * k;
+        psi[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (c < a.nchunk)
+          psi[k] = *reinterpret_cast<const float4 *>(a.ck_psi + (tr * NCK + b) * a.ldg + 4 * c);
+      }
+      // ---- recompute psi entering each segment of the block.  The loops over
+      // the block stay rolled (unrolled, the derivative code outgrows the
+      // instruction cache); each iteration issues the next segment's loads
+      // before its own arithmetic.
+      float z = a.ck_z[tr * NCK + b];
+      float ds = __ldg(dsb + n0);
+      Seg g = segment_geometry(a, z, checked_source(a, __ldg(srcb + n0), li));
+      AdjRows<CPL, QUAD> cur;
+#pragma unroll 1
+      for (int jj = 0; jj < cnt; ++jj) {
+        if (li == 0) {
+          s_geo[jj] = g;
+          s_ds[jj] = ds;
+        }
+        adj_load<CPL, QUAD, false>(a, x, g, li, TPW, cur);
+#pragma unroll
+        for (int k = 0; k < CPL; ++k) {
+          hist_base[(jj * CPL + k) * BLOCK] = psi[k];
+          const int c = li + TPW * k;
+          if (c >= a.nchunk) continue;
+#pragma unroll
+          for (int e = 0; e < 4; ++e) {
+            float p = get(psi[k], e);
+            const float q1r = get(cur.r1[k], e), q2r = q1r * q1r;
+            if (QUAD)
+              mixed_quad(a, get(cur.y[k][0], e), get(cur.y[k][QUAD ? 1 : 0], e),
+                         get(cur.y[k][QUAD ? 2 : 0], e), get(cur.sig[k], e), q1r, q2r, q1r * q2r,
+                         q2r * q2r * (1.0f / 3.0f), g.zin, ds, mu, mu2, w, p);
+            else
+              mixed_flat(get(cur.y[k][0], e), get(cur.sig[k], e), q1r, ds, w_mu, p);
+            set(psi[k], e, p);
+          }
+        }
+        if (jj + 1 < cnt) {
+          z = advance_z(a, z, ds, mu);
+          ds = __ldg(dsb + n0 + jj + 1);
+          g = segment_geometry(a, z, checked_source(a, __ldg(srcb + n0 + jj + 1), li));
+        }
+      }
+      __syncwarp();
+      // ---- reverse through the block
+#pragma unroll 1
+      for (int jj = cnt - 1; jj >= 0; --jj) {
+        g = s_geo[jj];
+        ds = s_ds[jj];
+        adj_load<CPL, QUAD, true>(a, x, g, li, TPW, cur);
+        const int mat = g.mat;
+#pragma unroll
+        for (int k = 0; k < CPL; ++k) {
+          const int c = li + TPW * k;
+          if (c >= a.nchunk) continue;
+          const int g4 = 4 * c;
+          const float4 ph = hist_base[(jj * CPL + k) * BLOCK];
+          float4 b1, b2, b3, sb;
+#pragma unroll
+          for (int e = 0; e < 4; ++e) {
+            const float abar = get(cur.lam[k], e) * (QUAD ? w : w_mu);
+            const AdjOut o =
+                QUAD ? adj_quad(a, get(cur.y[k][0], e), get(cur.y[k][QUAD ? 1 : 0], e),
+                                get(cur.y[k][QUAD ? 2 : 0], e), get(cur.sig[k], e),
+                                get(cur.r1[k], e), g.zin, ds, mu, mu2, get(ph, e),
+                                get(pbar[k], e), abar)
+                     : adj_flat(get(cur.y[k][0], e), get(cur.sig[k], e), get(cur.r1[k], e), ds,
+                                get(ph, e), get(pbar[k], e), abar);
+            set(pbar[k], e, o.pbar);
+            set(b1, e, o.y1b);
+            set(b2, e, o.y2b);
+            set(b3, e, o.y3b);
+            set(sb, e, g4 + e < a.G ? o.sbar : 0.f);
+          }
+          if (valid) {
+            if (acc) {
+              // one 16-byte read-modify-write per lane: the lanes of a
+              // sub-warp own distinct chunks of the row, sub-warps own slices
+              float4 *t = reinterpret_cast<float4 *>(acc + (int64_t)mat * a.ldg + g4);
+              float4 v = *t;
+              v.x += sb.x;
+              v.y += sb.y;
+              v.z += sb.z;
+              v.w += sb.w;
+              *t = v;
+            } else {
+#pragma unroll
+              for (int e = 0; e < 4; ++e)
+                if (g4 + e < a.G)
+                  atomicAdd(x.dsig + (int64_t)mat * a.ldg + g4 + e, (double)get(sb, e));
+            }
+            float *dq = x.dq + g.qrow + g4;
+            red_add_v4(dq, b1.x, b1.y, b1.z, b1.w);
+            if (QUAD) {
+              red_add_v4(dq + a.ldg, b2.x, b2.y, b2.z, b2.w);
+              red_add_v4(dq + 2 * a.ldg, b3.x, b3.y, b3.z, b3.w);
+            }
+          }
+        }
+      }
+      __syncwarp();
+    }
+    if (valid && x.dpsi_in) {
+#pragma unroll
+      for (int k = 0; k < CPL; ++k) {
+        const int c = li + TPW * k;
+        for (int e = 0; e < 4; ++e)
+          if (c < a.nchunk && 4 * c + e < a.G) x.dpsi_in[tr * a.G + 4 * c + e] = get(pbar[k], e);
+      }
+    }
+  }
+  if (x.slices) {
+    __syncthreads();
+    for (int64_t i = threadIdx.x; i < per_slice; i += BLOCK) {
+      double v = 0.0;
+      for (int sl = 0; sl < x.nsub; ++sl) v += (double)s_acc[sl * per_slice + i];
+      if (v != 0.0) atomicAdd(x.dsig + i, v);
+    }
+  }
+}
+
+
+template <int CPL, bool QUAD>
+int launch_adj_t(moc_problem *p, const AdjArgs &x, int tpw) {
+  auto kern = adjoint_kernel<CPL, QUAD>;
+  AdjArgs y = x;
+  y.tpw = tpw;
+  y.nsub = (BLOCK / 32) * (32 / tpw);
+  const size_t slice_bytes = sizeof(float) * (size_t)x.n_sigt * x.a.ldg * y.nsub;
+  const size_t fixed = adj_hist_bytes<CPL>() + (sizeof(Seg) + sizeof(float)) * y.nsub * ADJ_KMAX;
+  // per-track dL/dsigma_t accumulators in shared memory while two blocks still
+  // fit an SM (227 KB each at most, 228 KB an SM with 1 KB reserved a block);
+  // otherwise FP64 atomics straight to global memory
+  y.slices = fixed + slice_bytes <= 113 * 1024 ? 1 : 0;
+  const size_t smem = fixed + (y.slices ? slice_bytes : 0);
+  if (smem > 48 * 1024)
+    MOC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 0, sms = 0;
+  MOC_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BLOCK, smem));
+  MOC_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p->device));
+  if (per_sm < 1) return MOC_ERR_UNSUPPORTED;
+  const int gpw = 32 / tpw;
+  const int64_t warps = (x.a.n3d + gpw - 1) / gpw;
+  int64_t grid = (int64_t)per_sm * sms;
+  const int64_t need = (warps + 7) / 8;
+  if (grid > need) grid = need;
+  if (grid < 1) grid = 1;
+  kern<<<(unsigned)grid, BLOCK, smem, p->stream>>>(y);
+  MOC_CUDA_TRY(cudaGetLastError());
+  p->launches++;
+  return MOC_OK;
+}
+
+// Lanes per track of the reverse sweep: every lane holds one float4 chunk up
+// to 32 chunks (128 groups), two beyond (256 groups); p->adj_tpw/adj_cpl
+// override.
+template <bool QUAD>
+int dispatch_adj(moc_problem *p, const AdjArgs &x) {
+  const int nchunk = p->ldg / 4;
+  int cpl = nchunk <= 32 ? 1 : 2;
+  if (p->adj_cpl > 0) cpl = p->adj_cpl;
+  int tpw = p->adj_tpw > 0 ? p->adj_tpw : (nchunk + cpl - 1) / cpl;
+  if (tpw < 1 || tpw > 32 || (int64_t)tpw * cpl < nchunk) return MOC_ERR_UNSUPPORTED;
+  if (cpl == 1) return launch_adj_t<1, QUAD>(p, x, tpw);
+  if (cpl == 2) return launch_adj_t<2, QUAD>(p, x, tpw);
+  return MOC_ERR_UNSUPPORTED;
+}
+
+template <bool QUAD>
+int dispatch_ckpt(moc_problem *p, const SweepArgs &a) {
+  const int nchunk = p->ldg / 4;
+  if (nchunk <= 8) return launch_t<8, 1, MODE_MIXED, QUAD, false, true>(p, a);
+  if (nchunk <= 16) return launch_t<16, 1, MODE_MIXED, QUAD, false, true>(p, a);
+  if (nchunk <= 32) return launch_t<32, 1, MODE_MIXED, QUAD, false, true>(p, a);
+  if (nchunk <= 64) return launch_t<32, 2, MODE_MIXED, QUAD, false, true>(p, a);
+  return MOC_ERR_UNSUPPORTED;
+}
+
+}  // namespace
+
+// Forward sweep (MIXED) storing psi and the height every k segments.
+int moc_launch_sweep_ckpt(moc_problem *p, float *ck_psi, float *ck_z, int k, int nck) {
+  SweepArgs a = build_args(p);
+  a.phi_lo = nullptr;
+  a.ck_psi = ck_psi;
+  a.ck_z = ck_z;
+  a.ck_k = k;
+  a.ck_n = nck;
+  return p->d.axial_exp == 2 ? dispatch_ckpt<true>(p, a) : dispatch_ckpt<false>(p, a);
+}
+
+int moc_launch_adjoint(moc_problem *p, const float *ck_psi, const float *ck_z, int k, int nck,
+                       const float *dphi, float *dq, double *dsig, float *dpsi_in) {
+  if (k < 1 || k > ADJ_KMAX) return MOC_ERR_ARG;
+  AdjArgs x{};
+  x.a = build_args(p);
+  x.a.psi_scale = nullptr;
+  x.a.ck_psi = const_cast<float *>(ck_psi);
+  x.a.ck_z = const_cast<float *>(ck_z);
+  x.a.ck_k = k;
+  x.a.ck_n = nck;
+  x.dphi = dphi;
+  x.dq = dq;
+  x.dsig = dsig;
+  x.dpsi_in = dpsi_in;
+  x.n_sigt = p->d.n_sigt;
+  return p->d.axial_exp == 2 ? dispatch_adj<true>(p, x) : dispatch_adj<false>(p, x);
+}

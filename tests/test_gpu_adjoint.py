@@ -1,0 +1,209 @@
+"""GPU tests of the adjoint sweep and its torch.autograd.Function binding.
+
+* against the FP64 CPU adjoint (oracle_adjoint64) on the same inputs:
+  dL/dq and dL/dsigma_t normwise <= 1e-4 (the GPU runs the FP32 MIXED sweep);
+* against central finite differences (h = 1e-3 relative) of the FP64 GPU
+  sweep on 64 random parameters of the fixed-source loss -- sigma_t, scatter,
+  nu*SigmaF, fine source: <= 1e-4 relative;
+* the adjoint (forward with checkpoints + reverse) takes <= 3x the time of a
+  plain forward sweep on the adjoint workload geometry.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def _lib():
+    from simplemoc_gb300 import _lib as L
+    return L
+
+
+def _adjoint_spec(n2d=1024, z=300, axial_exp=2, seed=20260104):
+    import simplemoc_gb300 as sm
+    # the small problem's geometry with 40 groups
+    return sm.CONFIG_SMALL.with_(n_groups=40, n_tracks_2d=n2d, z_stacked=z, axial_exp=axial_exp,
+                                 seed=seed)
+
+
+# widths: automatic (3 lanes a track, 10 tracks a warp, 2 lanes idle), two
+# chunks a lane, one track a warp; 600 materials put the dL/dsigma_t
+# accumulators past shared memory (FP64 atomics to global memory instead)
+@pytest.mark.parametrize("axial_exp,width,n_materials", [
+    (2, (0, 0), 8), (0, (0, 0), 8), (2, (2, 2), 8), (0, (2, 2), 8), (2, (32, 1), 8),
+    (2, (0, 0), 600)])
+def test_adjoint_matches_fp64_cpu_adjoint(gpu_available, port, axial_exp, width, n_materials):
+    import torch
+
+    import simplemoc_gb300 as sm
+    L = _lib()
+    spec = sm.ProblemSpec(n_groups=12, fai=5, cai=4, height=200.0, n_sources=60, n_tracks_2d=12,
+                          n_polar=4, z_stacked=10, n_seg=50, axial_exp=axial_exp,
+                          n_materials=n_materials, seed=31)
+    hp = sm.generate(spec)
+    rng = np.random.default_rng(3)
+    dphi = rng.random(spec.n_fsr * spec.n_groups).astype(np.float32)
+    dev = torch.device("cuda", 0)
+    with sm.Solver(hp) as s:
+        lib, h = s._lib, s.handle
+        L.check(lib.moc_set_adjoint_width(h, *width), "width")
+        L.check(lib.moc_zero_state(h, 1, 1), "zero")
+        L.check(lib.moc_adjoint_forward(h, 8), "fwd")
+        dphi_t = torch.from_numpy(dphi).to(dev)
+        dq = torch.empty_like(dphi_t)
+        dsig = torch.empty(hp.sigt.size, dtype=torch.float64, device=dev)
+        dpsi = torch.empty(spec.n_tracks_3d * spec.n_groups, dtype=torch.float32, device=dev)
+        torch.cuda.synchronize()
+        L.check(lib.moc_adjoint_backward(h, dphi_t.data_ptr(), dq.data_ptr(), dsig.data_ptr(),
+                                         dpsi.data_ptr()), "bwd")
+        s.synchronize()
+        phi = s.download(fine_flux=True, fine_source=False, psi_f=False)["fine_flux"]
+    op = oracle.make_problem(hp)
+    q64 = hp.fine_source.astype(np.float64)
+    st = oracle.fresh_state(hp, np.float64)
+    port.sweep64(op, q64, st["fine_flux"], st["psi_f"])
+    rq, rs, rp = port.adjoint64(op, q64, dphi.astype(np.float64))
+    rel = lambda a, b: np.abs(a - b).max() / np.abs(b).max()
+    assert rel(phi, st["fine_flux"]) <= 1e-5
+    assert rel(dq.cpu().numpy(), rq) <= 1e-4
+    assert rel(dsig.cpu().numpy(), rs) <= 1e-4
+    assert rel(dpsi.cpu().numpy(), rp) <= 1e-4
+
+
+def test_adjoint_gradients_vs_central_differences(gpu_available):
+    """64 random parameters of the fixed-source loss, 16 of each kind."""
+    import torch
+
+    import simplemoc_gb300 as sm
+    from simplemoc_gb300.adjoint import FixedSourceLoss
+    L = _lib()
+    spec = _adjoint_spec(n2d=128)
+    hp = sm.generate(spec)
+    G, n_xs = spec.n_groups, hp.xs.size // (3 * spec.n_groups)
+    dev = torch.device("cuda", 0)
+    rng = np.random.default_rng(17)
+    phi0 = torch.from_numpy(rng.random((spec.n_sources, spec.fai, G))).to(dev)
+    sig0 = torch.from_numpy(hp.sigt.reshape(-1, G).copy())
+    S0 = torch.from_numpy(hp.scatter.reshape(n_xs, G, G).astype(np.float64)).to(dev)
+    nf0 = torch.from_numpy(hp.xs.reshape(n_xs, G, 3)[:, :, 0].astype(np.float64)).to(dev)
+    # fuel materials only have nu*SigmaF
+    s_ad = sm.Solver(hp)
+    fl = FixedSourceLoss(hp, s_ad)
+    sig = sig0.clone().requires_grad_(True)
+    S = S0.clone().requires_grad_(True)
+    nf = nf0.clone().requires_grad_(True)
+    loss, q = fl(sig, S, nf, phi0)
+    q.retain_grad()
+    loss.backward()
+    g_sig, g_S, g_nf, g_q = sig.grad.numpy(), S.grad.cpu().numpy(), nf.grad.cpu().numpy(), \
+        q.grad.cpu().numpy()
+
+    s64 = sm.Solver(hp, mode="fp64")
+    lib, h = s64._lib, s64.handle
+    NS, F = spec.n_sources, spec.fai
+
+    def weights(nusf):
+        return (fl.vol[:, None, None] * nusf[fl.src_xs][:, None, :]).expand(NS, F, G).reshape(-1)
+
+    w = weights(nf0)
+
+    def loss64(sigma=None, q64=None, nusf=None):
+        if sigma is not None:
+            L.check(lib.moc_set_sigma_t(h, L.ptr(np.ascontiguousarray(sigma, np.float32).ravel(),
+                                                 C.c_float)), "sig")
+        L.check(lib.moc_zero_state(h, 1, 1), "zero")
+        torch.cuda.synchronize()
+        L.check(lib.moc_set_fine_source64_device(h, q64.data_ptr()), "q64")
+        L.check(lib.moc_transport_sweep(h, None), "sweep")
+        phi = torch.empty(spec.n_fsr * G, dtype=torch.float64, device=dev)
+        L.check(lib.moc_get_fine_flux64_device(h, phi.data_ptr()), "phi")
+        s64.synchronize()
+        ww = w if nusf is None else weights(nusf)
+        return float((ww * phi).sum())
+
+    q_base = fl.source(phi0, S0, nf0).reshape(-1).contiguous()
+    h_rel = 1e-3
+    errs = []
+    fuel = [m for m in range(n_xs) if np.abs(hp.xs.reshape(n_xs, G, 3)[m, :, 0]).max() > 0]
+    for kind in ("sigma_t", "scatter", "nusf", "q"):
+        for _ in range(16):
+            if kind == "sigma_t":
+                m, g = int(rng.integers(sig0.shape[0])), int(rng.integers(G))
+                sp, sm_ = sig0.numpy().copy(), sig0.numpy().copy()
+                sp[m, g] = np.float32(sp[m, g] * (1 + h_rel))
+                sm_[m, g] = np.float32(sm_[m, g] * (1 - h_rel))
+                fd = (loss64(sigma=sp, q64=q_base) - loss64(sigma=sm_, q64=q_base)) / \
+                    (float(sp[m, g]) - float(sm_[m, g]))
+                loss64(sigma=sig0.numpy(), q64=q_base)
+                ad = g_sig[m, g]
+            elif kind == "scatter":
+                m, g, g2 = int(rng.integers(n_xs)), int(rng.integers(G)), int(rng.integers(G))
+                d = h_rel * float(S0[m, g, g2])
+                Sp, Sm = S0.clone(), S0.clone()
+                Sp[m, g, g2] += d
+                Sm[m, g, g2] -= d
+                fd = (loss64(q64=fl.source(phi0, Sp, nf0).reshape(-1).contiguous()) -
+                      loss64(q64=fl.source(phi0, Sm, nf0).reshape(-1).contiguous())) / (2 * d)
+                ad = g_S[m, g, g2]
+            elif kind == "nusf":
+                m, g = int(rng.choice(fuel)), int(rng.integers(G))
+                d = h_rel * float(nf0[m, g])
+                Np, Nm = nf0.clone(), nf0.clone()
+                Np[m, g] += d
+                Nm[m, g] -= d
+                fd = (loss64(q64=fl.source(phi0, S0, Np).reshape(-1).contiguous(), nusf=Np) -
+                      loss64(q64=fl.source(phi0, S0, Nm).reshape(-1).contiguous(), nusf=Nm)) / (2 * d)
+                ad = g_nf[m, g]
+            else:
+                k = int(rng.integers(q_base.numel()))
+                d = h_rel * float(q_base[k])
+                qp, qm = q_base.clone(), q_base.clone()
+                qp[k] += d
+                qm[k] -= d
+                fd = (loss64(q64=qp) - loss64(q64=qm)) / (2 * d)
+                ad = g_q[k]
+            errs.append((kind, abs(ad - fd) / abs(fd), ad, fd))
+    s_ad.close()
+    s64.close()
+    worst = max(errs, key=lambda e: e[1])
+    assert worst[1] <= 1e-4, worst
+
+
+def test_adjoint_time_within_three_forward_sweeps(gpu_available):
+    import torch
+
+    import simplemoc_gb300 as sm
+    L = _lib()
+    spec = _adjoint_spec()
+    hp = sm.generate(spec, with_state=False)
+    with sm.Solver(hp, mode="mixed") as s:
+        lib, h = s._lib, s.handle
+        s.time_sweep(1)
+        t_fwd = s.time_sweep(3)
+        dev = torch.device("cuda", 0)
+        dphi = torch.rand(spec.n_fsr * spec.n_groups, device=dev)
+        dq = torch.empty_like(dphi)
+        dsig = torch.empty(hp.sigt.size, dtype=torch.float64, device=dev)
+        import time
+        times, parts = [], []
+        for _ in range(3):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            L.check(lib.moc_adjoint_forward(h, 8), "fwd")
+            s.synchronize()
+            t1 = time.perf_counter()
+            L.check(lib.moc_adjoint_backward(h, dphi.data_ptr(), dq.data_ptr(), dsig.data_ptr(),
+                                             None), "bwd")
+            s.synchronize()
+            t2 = time.perf_counter()
+            times.append((t2 - t0) * 1e3)
+            parts.append(((t1 - t0) * 1e3, (t2 - t1) * 1e3))
+    best = int(np.argmin(times))
+    ratio = times[best] / t_fwd
+    print(f"forward sweep {t_fwd:.2f} ms, adjoint {times[best]:.2f} ms (forward with "
+          f"checkpoints {parts[best][0]:.2f} + reverse {parts[best][1]:.2f}), ratio {ratio:.2f}")
+    assert ratio <= 3.0
