@@ -138,7 +138,13 @@ int moc_create(const moc_dims *dims, const moc_host *host, int device,
                moc_problem **out);
 int moc_destroy(moc_problem *p);
 /* Re-uploads every input array of `host` into the existing storage (same
- * dims).  Used to time the host-to-device leg of a full call sequence. */
+ * dims).  The per-track arrays (seg_src, psi_f, psi_b) are copied on a second
+ * stream in up to 8 chunks of whole 2D tracks and the call returns with them
+ * in flight: the next moc_transport_sweep / moc_power_iteration sweeps each
+ * chunk as soon as it lands, and every other call waits for the copies first.
+ * The host arrays must stay unchanged until a call that waits for the device
+ * (moc_synchronize, moc_download, moc_power_iteration with outputs, ...) has
+ * returned.  Invalid source ids are rejected here (MOC_ERR_ARG). */
 int moc_upload(moc_problem *p, const moc_host *host);
 /* Copies results back (any pointer may be NULL to skip that array). */
 int moc_download(moc_problem *p, float *fine_flux, float *fine_source,

@@ -50,20 +50,21 @@ void dfree(T *&ptr) {
 }
 
 // Copies a [rows x G] host matrix into a [rows x ldg] device matrix.
-int put_rows(moc_problem *p, float *dst, const float *src, int64_t rows) {
+int put_rows(moc_problem *p, float *dst, const float *src, int64_t rows,
+             cudaStream_t st = nullptr) {
   const int64_t G = p->d.n_groups, L = p->ldg;
+  if (!st) st = p->stream;
   if (!src) {
-    MOC_CUDA_TRY(cudaMemsetAsync(dst, 0, sizeof(float) * (size_t)(rows * L), p->stream));
+    MOC_CUDA_TRY(cudaMemsetAsync(dst, 0, sizeof(float) * (size_t)(rows * L), st));
     return MOC_OK;
   }
   if (L == G) {
     MOC_CUDA_TRY(cudaMemcpyAsync(dst, src, sizeof(float) * (size_t)(rows * G),
-                                 cudaMemcpyHostToDevice, p->stream));
+                                 cudaMemcpyHostToDevice, st));
   } else {
-    MOC_CUDA_TRY(cudaMemsetAsync(dst, 0, sizeof(float) * (size_t)(rows * L), p->stream));
+    MOC_CUDA_TRY(cudaMemsetAsync(dst, 0, sizeof(float) * (size_t)(rows * L), st));
     MOC_CUDA_TRY(cudaMemcpy2DAsync(dst, sizeof(float) * L, src, sizeof(float) * G,
-                                   sizeof(float) * G, (size_t)rows, cudaMemcpyHostToDevice,
-                                   p->stream));
+                                   sizeof(float) * G, (size_t)rows, cudaMemcpyHostToDevice, st));
   }
   return MOC_OK;
 }
@@ -82,9 +83,9 @@ int get_rows(moc_problem *p, T *dst, const T *src, int64_t rows) {
 }
 
 template <typename T>
-int put(moc_problem *p, T *dst, const T *src, int64_t count) {
-  MOC_CUDA_TRY(
-      cudaMemcpyAsync(dst, src, sizeof(T) * (size_t)count, cudaMemcpyHostToDevice, p->stream));
+int put(moc_problem *p, T *dst, const T *src, int64_t count, cudaStream_t st = nullptr) {
+  MOC_CUDA_TRY(cudaMemcpyAsync(dst, src, sizeof(T) * (size_t)count, cudaMemcpyHostToDevice,
+                               st ? st : p->stream));
   return MOC_OK;
 }
 
@@ -95,7 +96,10 @@ int put(moc_problem *p, T *dst, const T *src, int64_t count) {
   } while (0)
 
 // Uploads every input and state array of `h` (validated) into the storage.
-int upload_all(moc_problem *p, const moc_host *h) {
+// With stream_tracks the per-track arrays go on the copy stream in chunks of
+// whole 2D tracks (events chunk_ev[k]) and the call returns with the upload in
+// flight; the next sweep starts on each chunk as it lands.
+int upload_all(moc_problem *p, const moc_host *h, bool stream_tracks) {
   const moc_dims &d = p->d;
   const int64_t N2D = d.n_tracks_2d, P = d.n_polar, S = d.n_seg, G = d.n_groups;
   const int64_t NS = d.n_sources;
@@ -112,7 +116,9 @@ int upload_all(moc_problem *p, const moc_host *h) {
   // the heights can reach (start heights and one wrap of [0, hd)).
   {
     float zmax = hd;
-    for (int64_t t = 0; t < p->n3d; ++t) zmax = h->z0[t] > zmax ? h->z0[t] : zmax;
+    const int64_t n3d = p->n3d;
+#pragma omp parallel for schedule(static) reduction(max : zmax)
+    for (int64_t t = 0; t < n3d; ++t) zmax = h->z0[t] > zmax ? h->z0[t] : zmax;
     const float dz = d.height / (float)(d.fai * d.decomp_ax * d.cai);
     const double lim = (double)zmax / (double)dz + 4.0;
     uint32_t m = (uint32_t)(0x100000000ull / (uint64_t)d.fai + 1ull);
@@ -124,7 +130,7 @@ int upload_all(moc_problem *p, const moc_host *h) {
     p->fmagic = m;
   }
   TRY(put(p, p->seg_ds, seg_ds.data(), N2D * P * S));
-  TRY(put(p, p->seg_src, h->seg_src, p->n3d * S));
+  if (!stream_tracks) TRY(put(p, p->seg_src, h->seg_src, p->n3d * S));
   TRY(put(p, p->weight, weight.data(), p->n3d));
   TRY(put(p, p->z0, h->z0, p->n3d));
   TRY(put(p, p->mu, mu.data(), P));
@@ -158,8 +164,30 @@ int upload_all(moc_problem *p, const moc_host *h) {
   }
   TRY(put_rows(p, p->q, h->fine_source, p->nfsr));
   TRY(put_rows(p, p->phi, h->fine_flux, p->nfsr));
-  TRY(put_rows(p, p->psi_f, h->psi_f, p->n3d));
-  TRY(put_rows(p, p->psi_b, h->psi_b, p->n3d));
+  if (stream_tracks) {
+    // the copies wait for the work already queued on the stream (a sweep may
+    // still read the arrays they overwrite)
+    MOC_CUDA_TRY(cudaEventRecord(p->main_ev, p->stream));
+    MOC_CUDA_TRY(cudaStreamWaitEvent(p->copy_stream, p->main_ev, 0));
+    const int n = (int)(N2D < moc_problem::MAX_UPLOAD_CHUNKS ? N2D : moc_problem::MAX_UPLOAD_CHUNKS);
+    const int64_t PZ = P * d.z_stacked;
+    for (int k = 0; k < n; ++k) {
+      const int64_t i0 = N2D * k / n, i1 = N2D * (k + 1) / n;
+      const int64_t t0 = i0 * PZ, nt = (i1 - i0) * PZ;
+      TRY(put(p, p->seg_src + t0 * S, h->seg_src + t0 * S, nt * S, p->copy_stream));
+      TRY(put_rows(p, p->psi_f + t0 * p->ldg, h->psi_f ? h->psi_f + t0 * G : nullptr, nt,
+                   p->copy_stream));
+      MOC_CUDA_TRY(cudaEventRecord(p->chunk_ev[k], p->copy_stream));
+      p->chunk_end[k] = i1;
+    }
+    TRY(put_rows(p, p->psi_b, h->psi_b, p->n3d, p->copy_stream));
+    MOC_CUDA_TRY(cudaEventRecord(p->copy_done, p->copy_stream));
+    p->n_chunks = n;
+  } else {
+    TRY(put(p, p->seg_src, h->seg_src, p->n3d * S));
+    TRY(put_rows(p, p->psi_f, h->psi_f, p->n3d));
+    TRY(put_rows(p, p->psi_b, h->psi_b, p->n3d));
+  }
   if (p->phi_lo)
     MOC_CUDA_TRY(cudaMemsetAsync(p->phi_lo, 0, sizeof(float) * (size_t)(p->nfsr * p->ldg), p->stream));
   // fresh FP64 state follows the uploaded FP32 state
@@ -172,7 +200,10 @@ int upload_all(moc_problem *p, const moc_host *h) {
   }
   p->psi_pending = false;
   TRY(moc_reset_psi_scale(p));
-  TRY(moc_detect_psi_b(p));
+  if (stream_tracks)
+    p->detect_pending = true;          // psi_b is still being copied
+  else
+    TRY(moc_detect_psi_b(p));
   MOC_CUDA_TRY(cudaMemsetAsync(p->err, 0, sizeof(int32_t), p->stream));
   return MOC_OK;
 }
@@ -187,9 +218,16 @@ void release(moc_problem *p) {
   dfree(p->ck_psi); dfree(p->ck_z); dfree(p->adj_dphi); dfree(p->adj_dq); dfree(p->adj_dsig);
   if (p->ev0) cudaEventDestroy(p->ev0);
   if (p->ev1) cudaEventDestroy(p->ev1);
+  if (p->copy_stream) cudaStreamSynchronize(p->copy_stream);
+  for (cudaEvent_t &e : p->chunk_ev)
+    if (e) cudaEventDestroy(e);
+  if (p->main_ev) cudaEventDestroy(p->main_ev);
+  if (p->copy_done) cudaEventDestroy(p->copy_done);
+  if (p->copy_stream) cudaStreamDestroy(p->copy_stream);
   if (p->stream) cudaStreamDestroy(p->stream);
-  p->ev0 = p->ev1 = nullptr;
-  p->stream = nullptr;
+  p->ev0 = p->ev1 = p->main_ev = p->copy_done = nullptr;
+  p->copy_stream = p->stream = nullptr;
+  p->n_chunks = 0;
 }
 
 // Records a failure on the handle; later calls report MOC_ERR_STATE.
@@ -202,6 +240,15 @@ int usable(const moc_problem *p) {
   if (!p) return MOC_ERR_ARG;
   if (p->status != MOC_OK) return MOC_ERR_STATE;
   return MOC_OK;
+}
+
+// Entry-point guard: a usable handle whose stream has joined any upload in
+// flight.
+int ready(moc_problem *p) {
+  int rc = usable(p);
+  if (rc != MOC_OK) return rc;
+  rc = moc_join_upload(p);
+  return rc == MOC_OK ? MOC_OK : fail(p, rc);
 }
 
 // Waits for the stream and folds the device error word into the status.
@@ -225,7 +272,20 @@ int read_scalars(moc_problem *p, double *out) {
 
 int sweep_impl(moc_problem *p) {
   const bool had_pending = p->psi_pending && p->mode != MOC_MODE_FP64;
-  int rc = moc_launch_sweep(p);
+  int rc = MOC_OK;
+  if (p->n_chunks > 0 && p->mode != MOC_MODE_FP64) {
+    // sweep each chunk of 2D tracks once its copy has landed
+    int64_t i0 = 0;
+    for (int k = 0; k < p->n_chunks && rc == MOC_OK; ++k) {
+      if (cudaStreamWaitEvent(p->stream, p->chunk_ev[k], 0) != cudaSuccess) return fail(p, MOC_ERR_CUDA);
+      rc = moc_launch_sweep_range(p, i0, p->chunk_end[k]);
+      i0 = p->chunk_end[k];
+    }
+    if (rc == MOC_OK) rc = moc_join_upload(p);
+  } else {
+    rc = moc_join_upload(p);
+    if (rc == MOC_OK) rc = moc_launch_sweep(p);
+  }
   if (rc != MOC_OK) return fail(p, rc);
   if (had_pending) {                   // the sweep applied it
     p->psi_pending = false;
@@ -241,6 +301,17 @@ int sweep_impl(moc_problem *p) {
 }
 
 }  // namespace
+
+int moc_join_upload(moc_problem *p) {
+  if (p->n_chunks == 0) return MOC_OK;
+  p->n_chunks = 0;
+  MOC_CUDA_TRY(cudaStreamWaitEvent(p->stream, p->copy_done, 0));
+  if (p->detect_pending) {
+    p->detect_pending = false;
+    return moc_detect_psi_b(p);
+  }
+  return MOC_OK;
+}
 
 extern "C" {
 
@@ -280,7 +351,13 @@ int moc_create(const moc_dims *dims, const moc_host *host, int device, moc_probl
   const int64_t N2D = dims->n_tracks_2d, P = dims->n_polar, S = dims->n_seg;
   const int64_t G = dims->n_groups, NS = dims->n_sources;
   rc = MOC_OK;
-  if (cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking) != cudaSuccess ||
+  bool ev_ok = true;
+  for (cudaEvent_t &e : p->chunk_ev)
+    ev_ok = ev_ok && cudaEventCreateWithFlags(&e, cudaEventDisableTiming) == cudaSuccess;
+  if (!ev_ok || cudaStreamCreateWithFlags(&p->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&p->copy_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&p->main_ev, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&p->copy_done, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreate(&p->ev0) != cudaSuccess || cudaEventCreate(&p->ev1) != cudaSuccess)
     rc = MOC_ERR_CUDA;
   if (rc == MOC_OK) rc = dalloc(p, &p->seg_ds, N2D * P * S);
@@ -313,7 +390,7 @@ int moc_create(const moc_dims *dims, const moc_host *host, int device, moc_probl
     if (cudaMemcpy(p->scalars, init, sizeof init, cudaMemcpyHostToDevice) != cudaSuccess)
       rc = MOC_ERR_CUDA;
   }
-  if (rc == MOC_OK) rc = upload_all(p, host);
+  if (rc == MOC_OK) rc = upload_all(p, host, false);
   if (rc == MOC_OK && cudaStreamSynchronize(p->stream) != cudaSuccess) rc = MOC_ERR_CUDA;
   if (rc != MOC_OK) {
     release(p);
@@ -327,6 +404,7 @@ int moc_create(const moc_dims *dims, const moc_host *host, int device, moc_probl
 int moc_destroy(moc_problem *p) {
   if (!p) return MOC_ERR_ARG;
   cudaSetDevice(p->device);
+  if (p->copy_stream) cudaStreamSynchronize(p->copy_stream);
   if (p->stream) cudaStreamSynchronize(p->stream);
   release(p);
   delete p;
@@ -334,18 +412,19 @@ int moc_destroy(moc_problem *p) {
 }
 
 int moc_upload(moc_problem *p, const moc_host *host) {
-  int rc = usable(p);
+  int rc = ready(p);
   if (rc != MOC_OK) return rc;
   if (!host) return MOC_ERR_ARG;
   rc = moc_host_validate(&p->d, host);
   if (rc != MOC_OK) return rc;
-  rc = upload_all(p, host);
+  // FP64 state is widened from the uploaded FP32 state at once: no streaming
+  rc = upload_all(p, host, p->q64 == nullptr);
   if (rc != MOC_OK) return fail(p, rc);
   return MOC_OK;
 }
 
 int moc_download(moc_problem *p, float *fine_flux, float *fine_source, float *psi_f, float *psi_b) {
-  int rc = usable(p);
+  int rc = ready(p);
   if (rc != MOC_OK) return rc;
   if (psi_f && p->psi_pending) {
     rc = moc_psi_materialize(p);
@@ -363,7 +442,7 @@ int moc_download(moc_problem *p, float *fine_flux, float *fine_source, float *ps
 
 int moc_download64(moc_problem *p, double *fine_flux, double *fine_source, double *psi_f,
                    double *psi_b) {
-  int rc = usable(p);
+  int rc = ready(p);
   if (rc != MOC_OK) return rc;
   if (!p->q64) return MOC_ERR_STATE;
   rc = sync_check(p);
@@ -383,7 +462,7 @@ int64_t moc_device_bytes(const moc_problem *p) { return p ? p->bytes : 0; }
 int64_t moc_launch_count(const moc_problem *p) { return p ? p->launches : 0; }
 
 int moc_set_mode(moc_problem *p, int mode, int flags) {
-  int rc = usable(p);
+  int rc = ready(p);
   if (rc != MOC_OK) return rc;
   if (mode != MOC_MODE_PLAIN && mode != MOC_MODE_MIXED && mode != MOC_MODE_FP64) return MOC_ERR_ARG;
   if (flags & ~MOC_FLAG_COMPENSATED) return MOC_ERR_ARG;
@@ -459,7 +538,7 @@ int moc_get_launch(const moc_problem *p, int *threads_per_track, int *chunks_per
 
 int moc_autotune(moc_problem *p, int64_t n_tracks, int *threads_per_track,
                  int *chunks_per_thread, double *ms_best) {
-  int rc = usable(p);
+  int rc = ready(p);
   if (rc != MOC_OK) return rc;
   cudaSetDevice(p->device);
   int tpw = 0, cpl = 0;
@@ -483,7 +562,7 @@ int moc_transport_sweep(moc_problem *p, int64_t *segments_processed) {
 }
 
 int moc_renormalize_flux(moc_problem *p) {
-  int rc = usable(p);
+  int rc = ready(p);
   if (rc != MOC_OK) return rc;
   cudaSetDevice(p->device);
   rc = moc_launch_renormalize(p);
@@ -491,7 +570,7 @@ int moc_renormalize_flux(moc_problem *p) {
 }
 
 int moc_update_sources(moc_problem *p, double keff, double *residual) {
-  int rc = usable(p);
+  int rc = ready(p);
   if (rc != MOC_OK) return rc;
   if (!(keff != 0.0)) return MOC_ERR_ARG;
   cudaSetDevice(p->device);
@@ -507,7 +586,7 @@ int moc_update_sources(moc_problem *p, double keff, double *residual) {
 }
 
 int moc_compute_keff(moc_problem *p, double leakage, double *keff) {
-  int rc = usable(p);
+  int rc = ready(p);
   if (rc != MOC_OK) return rc;
   cudaSetDevice(p->device);
   rc = moc_launch_keff(p, leakage);
@@ -541,13 +620,13 @@ int moc_power_iteration(moc_problem *p, double keff_in, double *keff_out, double
 }
 
 int moc_synchronize(moc_problem *p) {
-  int rc = usable(p);
+  int rc = ready(p);
   if (rc != MOC_OK) return rc;
   return sync_check(p);
 }
 
 int moc_time_sweep(moc_problem *p, int iters, double *ms_per_sweep) {
-  int rc = usable(p);
+  int rc = ready(p);
   if (rc != MOC_OK) return rc;
   if (iters < 1 || !ms_per_sweep) return MOC_ERR_ARG;
   cudaSetDevice(p->device);
@@ -568,7 +647,7 @@ int moc_time_sweep(moc_problem *p, int iters, double *ms_per_sweep) {
 
 int moc_time_power_iterations(moc_problem *p, int iters, double *ms_total, double *ms_sweeps,
                               double *keff, double *residual) {
-  int rc = usable(p);
+  int rc = ready(p);
   if (rc != MOC_OK) return rc;
   if (iters < 1) return MOC_ERR_ARG;
   cudaSetDevice(p->device);
@@ -629,7 +708,7 @@ int copy_rows_dd(moc_problem *p, T *dst, int64_t dpitch, const T *src, int64_t s
 extern "C" {
 
 int moc_set_fine_source_device(moc_problem *p, const float *q) {
-  int rc = usable(p);
+  int rc = ready(p);
   if (rc != MOC_OK) return rc;
   if (!q) return MOC_ERR_ARG;
   cudaSetDevice(p->device);
@@ -643,7 +722,7 @@ int moc_set_fine_source_device(moc_problem *p, const float *q) {
 }
 
 int moc_set_fine_source64_device(moc_problem *p, const double *q) {
-  int rc = usable(p);
+  int rc = ready(p);
   if (rc != MOC_OK) return rc;
   if (!q || !p->q64) return !q ? MOC_ERR_ARG : MOC_ERR_STATE;
   cudaSetDevice(p->device);
@@ -652,7 +731,7 @@ int moc_set_fine_source64_device(moc_problem *p, const double *q) {
 }
 
 int moc_set_sigma_t(moc_problem *p, const float *sigt) {
-  int rc = usable(p);
+  int rc = ready(p);
   if (rc != MOC_OK) return rc;
   if (!sigt) return MOC_ERR_ARG;
   for (int64_t k = 0; k < (int64_t)p->d.n_sigt * p->d.n_groups; ++k)
@@ -666,7 +745,7 @@ int moc_set_sigma_t(moc_problem *p, const float *sigt) {
 }
 
 int moc_zero_state(moc_problem *p, int flux, int psi) {
-  int rc = usable(p);
+  int rc = ready(p);
   if (rc != MOC_OK) return rc;
   cudaSetDevice(p->device);
   const size_t fb = sizeof(float) * (size_t)(p->nfsr * p->ldg);
@@ -693,7 +772,7 @@ int moc_zero_state(moc_problem *p, int flux, int psi) {
 }
 
 int moc_get_fine_flux_device(moc_problem *p, float *phi) {
-  int rc = usable(p);
+  int rc = ready(p);
   if (rc != MOC_OK) return rc;
   if (!phi) return MOC_ERR_ARG;
   cudaSetDevice(p->device);
@@ -702,7 +781,7 @@ int moc_get_fine_flux_device(moc_problem *p, float *phi) {
 }
 
 int moc_get_fine_flux64_device(moc_problem *p, double *phi) {
-  int rc = usable(p);
+  int rc = ready(p);
   if (rc != MOC_OK) return rc;
   if (!phi || !p->phi64) return !phi ? MOC_ERR_ARG : MOC_ERR_STATE;
   cudaSetDevice(p->device);
@@ -713,7 +792,7 @@ int moc_get_fine_flux64_device(moc_problem *p, double *phi) {
 // ---- adjoint ---------------------------------------------------------------
 
 int moc_adjoint_forward(moc_problem *p, int k_ckpt) {
-  int rc = usable(p);
+  int rc = ready(p);
   if (rc != MOC_OK) return rc;
   if (k_ckpt < 1 || k_ckpt > 8) return MOC_ERR_ARG;
   if (p->d.n_groups > 256) return MOC_ERR_UNSUPPORTED;
@@ -741,7 +820,7 @@ int moc_adjoint_forward(moc_problem *p, int k_ckpt) {
 
 int moc_adjoint_backward(moc_problem *p, const float *dphi, float *dq, double *dsigt,
                          float *dpsi_in) {
-  int rc = usable(p);
+  int rc = ready(p);
   if (rc != MOC_OK) return rc;
   if (!dphi || !p->ck_psi) return !dphi ? MOC_ERR_ARG : MOC_ERR_STATE;
   cudaSetDevice(p->device);

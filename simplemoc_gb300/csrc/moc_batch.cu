@@ -129,6 +129,18 @@ int batch_post(moc_batch *b) {
   return MOC_OK;
 }
 
+// A core uploaded since the batch last ran: its copies must land (and its
+// stream drain) before the batch stream reads its arrays.
+int join_cores(moc_batch *b) {
+  for (moc_problem *p : b->cores) {
+    if (p->n_chunks == 0) continue;
+    int rc = moc_join_upload(p);
+    if (rc != MOC_OK) return rc;
+    MOC_CUDA_TRY(cudaStreamSynchronize(p->stream));
+  }
+  return MOC_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -169,8 +181,10 @@ int moc_batch_create(int n, moc_problem *const *problems, moc_batch **out) {
       cudaMalloc(&b->d_counter, sizeof(unsigned long long)) != cudaSuccess)
     rc = MOC_ERR_CUDA;
   // make every core's previous work visible to the batch stream
-  for (moc_problem *p : b->cores)
+  for (moc_problem *p : b->cores) {
+    if (rc == MOC_OK) rc = moc_join_upload(p);
     if (rc == MOC_OK && cudaStreamSynchronize(p->stream) != cudaSuccess) rc = MOC_ERR_CUDA;
+  }
   if (rc == MOC_OK) rc = rebuild_tasks(b);
   if (rc != MOC_OK) {
     moc_batch_destroy(b);
@@ -304,7 +318,8 @@ int moc_batch_autotune(moc_batch *b) {
 int moc_batch_sweep(moc_batch *b) {
   if (!b) return MOC_ERR_ARG;
   cudaSetDevice(b->device);
-  int rc = batch_sweep(b);
+  int rc = join_cores(b);
+  if (rc == MOC_OK) rc = batch_sweep(b);
   if (rc != MOC_OK) return rc;
   MOC_CUDA_TRY(cudaStreamSynchronize(b->stream));
   return MOC_OK;
@@ -316,7 +331,8 @@ int moc_batch_sweep(moc_batch *b) {
 int moc_batch_power_iterations(moc_batch *b, int iters, int use_graph, double *ms_total) {
   if (!b || iters < 1) return MOC_ERR_ARG;
   cudaSetDevice(b->device);
-  int rc = MOC_OK;
+  int rc = join_cores(b);
+  if (rc != MOC_OK) return rc;
   if (use_graph && !b->exec) {
     // one eager iteration first: kernel attributes are set and every core has
     // a pending renormalisation, the steady state the graph replays

@@ -101,12 +101,27 @@ struct moc_problem {
   int32_t *err = nullptr;
   int32_t red_blocks = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // Upload of the per-track arrays (segment sources, psi_f, psi_b) on a copy
+  // stream in chunks of whole 2D tracks, so that the next sweep starts on the
+  // first chunk while the rest are still copied.  n_chunks > 0 while an upload
+  // is in flight; every other entry point first joins it (moc_join_upload).
+  static constexpr int MAX_UPLOAD_CHUNKS = 8;
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t main_ev = nullptr, copy_done = nullptr;
+  cudaEvent_t chunk_ev[MAX_UPLOAD_CHUNKS] = {};
+  int64_t chunk_end[MAX_UPLOAD_CHUNKS] = {};     // one past the chunk's last 2D track
+  int n_chunks = 0;
+  bool detect_pending = false;                   // psi_b's nonzero flag still to be set
   // host copies needed for re-upload and derived arrays
   float polar[64];
 };
 
 // Launchers implemented in moc_sweep.cu / moc_post.cu.
 int moc_launch_sweep(moc_problem *p);
+// The sweep of 2D tracks [i2_begin, i2_end) with all their 3D tracks.
+int moc_launch_sweep_range(moc_problem *p, int64_t i2_begin, int64_t i2_end);
+// Makes the stream wait for an upload in flight (no-op when there is none).
+int moc_join_upload(moc_problem *p);
 int moc_launch_sweep_csr(moc_problem *p, const int64_t *off, const float *ds, const float *z,
                          const int32_t *src);
 SweepArgs moc_sweep_args(moc_problem *p);

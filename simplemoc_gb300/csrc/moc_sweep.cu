@@ -737,6 +737,27 @@ int moc_launch_sweep(moc_problem *p) {
   return launch_args(p, build_args(p), tpw, cpl);
 }
 
+// A range of whole 2D tracks is a contiguous range of 3D tracks (the track
+// index is (i2 * P + polar) * Z + stack), so the sweep of the range is the
+// sweep kernel over per-track arrays offset to its first track.
+int moc_launch_sweep_range(moc_problem *p, int64_t i2_begin, int64_t i2_end) {
+  const int64_t P = p->d.n_polar, Z = p->d.z_stacked, S = p->d.n_seg;
+  if (i2_begin < 0 || i2_end > p->d.n_tracks_2d || i2_begin >= i2_end) return MOC_ERR_ARG;
+  if (p->mode == MOC_MODE_FP64) return MOC_ERR_UNSUPPORTED;
+  int tpw = 0, cpl = 0;
+  int st = moc_sweep_launch_shape(p, &tpw, &cpl);
+  if (st != MOC_OK) return st;
+  SweepArgs a = build_args(p);
+  const int64_t t0 = i2_begin * P * Z;
+  a.seg_ds += i2_begin * P * S;
+  a.seg_src += t0 * S;
+  a.weight += t0;
+  a.z0 += t0;
+  a.psi += t0 * p->ldg;
+  a.n3d = (i2_end - i2_begin) * P * Z;
+  return launch_args(p, a, tpw, cpl);
+}
+
 // Times every launch shape that covers the groups on the first n_sub tracks.
 // Tallies go to a scratch copy of the flux array and the tracks' angular flux
 // to a scratch copy, so the problem's state is not changed.

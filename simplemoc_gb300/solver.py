@@ -82,8 +82,12 @@ class Solver:
         return a.value, b.value, ms.value
 
     def upload(self, problem: HostProblem | None = None) -> None:
+        """Copies `problem` (default: the problem the solver was made with) to
+        the device.  The per-track copies may still be in flight when this
+        returns; the arrays are kept referenced until the next upload."""
         p = problem or self.problem
         self._host = p.host()
+        self._host_problem = p
         L.check(self._lib.moc_upload(self._h, C.byref(self._host)), "moc_upload")
 
     # ---- the four reference entry points ------------------------------------
