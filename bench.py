@@ -52,7 +52,12 @@ def _args():
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0,
                     help="target CPU time of one reference-arm sample")
-    return ap.parse_args()
+    ap.add_argument("--launch", default=None, metavar="TPW,CPL",
+                    help="fixed sweep launch shape (threads per track, chunks per thread) "
+                         "instead of the autotuner's")
+    a = ap.parse_args()
+    a.launch = tuple(int(v) for v in a.launch.split(",")) if a.launch else None
+    return a
 
 
 def _dist():
@@ -381,7 +386,13 @@ def main():
     ints = spec.integrations_per_sweep
 
     # ---- chosen (MIXED) ------------------------------------------------------
-    shapes = {"mixed": list(solver.autotune()[:2])}
+    def tune():
+        if args.launch:
+            solver.set_launch(*args.launch)
+            return list(args.launch)
+        return list(solver.autotune()[:2])
+
+    shapes = {"mixed": tune()}
     if W:
         solver.time_power_iterations(W)
     barrier()
@@ -400,13 +411,16 @@ def main():
 
     # ---- plain (reference arithmetic) ------------------------------------------
     solver.set_mode("plain")
-    shapes["plain"] = list(solver.autotune()[:2])
+    shapes["plain"] = tune()
     solver.time_power_iterations(1)
     rp = solver.time_power_iterations(K)
     plain_value = ints * K / (rp["ms_total"] / 1e3)
     plain_sweep_ms = rp["ms_sweeps"] / K
     solver.set_mode("mixed")
-    solver.autotune(measure=False)
+    if args.launch:
+        solver.set_launch(*args.launch)
+    else:
+        solver.autotune(measure=False)
 
     # ---- end to end through the C ABI with host buffers ------------------------
     e2e = None
