@@ -57,6 +57,10 @@ extern "C" {
 
 /* mode flags */
 #define MOC_FLAG_COMPENSATED 0x1  /* MIXED: compensated (hi/lo) FSR tallies  */
+/* MIXED runs update_sources' scatter/fission contraction on the tensor cores
+ * (split TF32, FP32 accumulation; up to 104 groups); this flag keeps it on the
+ * CUDA cores instead. */
+#define MOC_FLAG_SIMT_UPDATE 0x2
 
 /* ---- problem description ---------------------------------------------- */
 typedef struct moc_dims {

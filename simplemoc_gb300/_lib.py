@@ -25,6 +25,7 @@ MOC_MODE_PLAIN = 0
 MOC_MODE_MIXED = 1
 MOC_MODE_FP64 = 2
 MOC_FLAG_COMPENSATED = 0x1
+MOC_FLAG_SIMT_UPDATE = 0x2
 
 f32p = C.POINTER(C.c_float)
 f64p = C.POINTER(C.c_double)

@@ -159,6 +159,36 @@ int upload_all(moc_problem *p, const moc_host *h, bool stream_tracks) {
     p->n_upd_items = (int32_t)(items.size() / 3);
     TRY(put(p, p->xs_order, order.data(), NS));
     TRY(put(p, p->upd_items, items.data(), (int64_t)items.size()));
+    // tensor-core tiles: <= 128 fine regions (128 / F sources) of one material,
+    // and per material the split second operand (scatter rows, nuSigmaF, SigmaA)
+    std::vector<int32_t> tc_items;
+    std::vector<float> tc_b;
+    if (p->tc_b) {
+      const int64_t per = 128 / d.fai;
+      for (int32_t m = 0; m < d.n_xs; ++m)
+        for (int64_t a = start[(size_t)m]; a < start[(size_t)m + 1]; a += per) {
+          const int64_t b = a + per < start[(size_t)m + 1] ? a + per : start[(size_t)m + 1];
+          tc_items.push_back(m);
+          tc_items.push_back((int32_t)a);
+          tc_items.push_back((int32_t)b);
+        }
+      const int kp = p->tc_kp, np = p->tc_np;
+      const int64_t plane = (int64_t)np * kp;
+      tc_b.assign((size_t)(d.n_xs * 2 * plane), 0.0f);
+      for (int64_t m = 0; m < d.n_xs; ++m)
+        for (int n = 0; n < G + 2; ++n)
+          for (int k = 0; k < G; ++k) {
+            const float v = n < G ? h->scatter[(m * G + n) * G + k]            // S[m][to n][from k]
+                                  : h->xs[(m * G + k) * 3 + (n - G)];          // nuSigmaF, SigmaA
+            const float hi = moc_tf32_rna(v);
+            const int64_t o = m * 2 * plane + moc_tc_b_offset(n, k, np);
+            tc_b[(size_t)o] = hi;
+            tc_b[(size_t)(o + plane)] = moc_tf32_rna(v - hi);
+          }
+      p->n_tc_items = (int32_t)(tc_items.size() / 3);
+      TRY(put(p, p->tc_items, tc_items.data(), (int64_t)tc_items.size()));
+      TRY(put(p, p->tc_b, tc_b.data(), (int64_t)tc_b.size()));
+    }
     // the pageable sources above must be consumed before the vectors go away
     MOC_CUDA_TRY(cudaStreamSynchronize(p->stream));
   }
@@ -216,6 +246,7 @@ void release(moc_problem *p) {
   dfree(p->psi_b64); dfree(p->partials); dfree(p->scalars); dfree(p->err);
   dfree(p->xs_order); dfree(p->upd_items); dfree(p->psi_scale); dfree(p->psi_b_nonzero);
   dfree(p->ck_psi); dfree(p->ck_z); dfree(p->adj_dphi); dfree(p->adj_dq); dfree(p->adj_dsig);
+  dfree(p->tc_b); dfree(p->tc_items);
   if (p->ev0) cudaEventDestroy(p->ev0);
   if (p->ev1) cudaEventDestroy(p->ev1);
   if (p->copy_stream) cudaStreamSynchronize(p->copy_stream);
@@ -258,6 +289,7 @@ int sync_check(moc_problem *p) {
   int32_t err = 0;
   e = cudaMemcpy(&err, p->err, sizeof(int32_t), cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return fail(p, MOC_ERR_CUDA);
+  if (err & 2) return fail(p, MOC_ERR_TIMEOUT);   // a bounded device wait gave up
   if (err != 0) return fail(p, MOC_ERR_ARG);
   return MOC_OK;
 }
@@ -376,6 +408,11 @@ int moc_create(const moc_dims *dims, const moc_host *host, int device, moc_probl
   if (rc == MOC_OK) rc = dalloc(p, &p->psi_scale, 1);
   if (rc == MOC_OK) rc = dalloc(p, &p->psi_b_nonzero, 1);
   if (rc == MOC_OK) rc = dalloc(p, &p->upd_items, 3 * ((int64_t)dims->n_xs + NS / 128 + 1));
+  if (rc == MOC_OK && moc_tc_dims(dims->n_groups, dims->fai, &p->tc_kp, &p->tc_np)) {
+    const int64_t per = 128 / dims->fai;
+    rc = dalloc(p, &p->tc_items, 3 * ((int64_t)dims->n_xs + NS / per + 1));
+    if (rc == MOC_OK) rc = dalloc(p, &p->tc_b, (int64_t)dims->n_xs * 2 * p->tc_np * p->tc_kp);
+  }
   if (rc == MOC_OK) rc = dalloc(p, &p->q, p->nfsr * p->ldg);
   if (rc == MOC_OK) rc = dalloc(p, &p->phi, p->nfsr * p->ldg);
   if (rc == MOC_OK) rc = dalloc(p, &p->psi_f, p->n3d * p->ldg);
@@ -465,7 +502,7 @@ int moc_set_mode(moc_problem *p, int mode, int flags) {
   int rc = ready(p);
   if (rc != MOC_OK) return rc;
   if (mode != MOC_MODE_PLAIN && mode != MOC_MODE_MIXED && mode != MOC_MODE_FP64) return MOC_ERR_ARG;
-  if (flags & ~MOC_FLAG_COMPENSATED) return MOC_ERR_ARG;
+  if (flags & ~(MOC_FLAG_COMPENSATED | MOC_FLAG_SIMT_UPDATE)) return MOC_ERR_ARG;
   if (p->psi_pending) {
     rc = moc_psi_materialize(p);
     if (rc != MOC_OK) return fail(p, rc);

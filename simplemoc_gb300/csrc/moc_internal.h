@@ -5,6 +5,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <cstring>
+
 #include "simplemoc_gb300.h"
 
 // Coefficients stored per (sigma_t row, group), as 8 planes of ldg floats:
@@ -89,6 +91,13 @@ struct moc_problem {
   // device flag psi_b_nonzero is set
   float *psi_scale = nullptr;
   int32_t *psi_b_nonzero = nullptr;
+  // tensor-core update_sources (MIXED): per material the split operand
+  // [hi, lo][tc_np x tc_kp] in the canonical layout, and tiles of <= 128 / F
+  // sources of one material (material, first, end) in xs_order
+  float *tc_b = nullptr;
+  int32_t *tc_items = nullptr;
+  int32_t n_tc_items = 0;
+  int tc_kp = 0, tc_np = 0;             // 0: groups beyond the tensor-core path
   bool psi_pending = false;
   // adjoint: psi checkpoints of the last moc_adjoint_forward and work arrays
   float *ck_psi = nullptr, *ck_z = nullptr;
@@ -122,6 +131,34 @@ int moc_launch_sweep(moc_problem *p);
 int moc_launch_sweep_range(moc_problem *p, int64_t i2_begin, int64_t i2_end);
 // Makes the stream wait for an upload in flight (no-op when there is none).
 int moc_join_upload(moc_problem *p);
+
+// Tensor-core update_sources.  The second operand of tile GEMM for material m
+// is B[n][k] (n < G: scatter S[m][n][k]; n = G: nuSigmaF[m][k]; n = G + 1:
+// SigmaA[m][k]; zero elsewhere), K-major in 8-row x 16-byte core matrices:
+// element (n, k) at float offset (k / 4) * np * 4 + n * 4 + k % 4.
+constexpr int MOC_TC_MAX_NP = 112;
+inline bool moc_tc_dims(int G, int F, int *kp, int *np) {
+  const int k = (G + 7) / 8 * 8, n = (G + 2 + 15) / 16 * 16;
+  if (G < 1 || k > 104 || n > MOC_TC_MAX_NP || F < 1 || F > 128) return false;
+  *kp = k;
+  *np = n;
+  return true;
+}
+// x rounded to TF32 (10-bit significand), to nearest with ties away from zero,
+// as cvt.rna.tf32.f32 does on the device.
+inline float moc_tf32_rna(float x) {
+  uint32_t u;
+  std::memcpy(&u, &x, 4);
+  if ((u & 0x7F800000u) == 0x7F800000u) return x;     // inf, nan
+  u = (u + 0x1000u) & 0xFFFFE000u;
+  float r;
+  std::memcpy(&r, &u, 4);
+  return r;
+}
+inline int64_t moc_tc_b_offset(int n, int k, int np) {
+  return (int64_t)(k / 4) * np * 4 + (int64_t)n * 4 + k % 4;
+}
+int moc_launch_update_tc(moc_problem *p);
 int moc_launch_sweep_csr(moc_problem *p, const int64_t *off, const float *ds, const float *z,
                          const int32_t *src);
 SweepArgs moc_sweep_args(moc_problem *p);

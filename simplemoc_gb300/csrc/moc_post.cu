@@ -454,6 +454,15 @@ __global__ void __launch_bounds__(RTHREADS) update_tiled_kernel(
 template <typename T>
 int update_t(moc_problem *p, const T *phi, T *q, bool with_keff) {
   const moc_dims &d = p->d;
+  if (sizeof(T) == 4 && p->mode == MOC_MODE_MIXED && !(p->flags & MOC_FLAG_SIMT_UPDATE) &&
+      p->tc_b && (const void *)phi == (const void *)p->phi && (const void *)q == (const void *)p->q) {
+    const int rc = moc_launch_update_tc(p);
+    if (rc != MOC_OK) return rc;
+    update_finalize<<<1, 32, 0, p->stream>>>(p->partials, p->scalars, 1, with_keff ? 1 : 0);
+    MOC_CUDA_TRY(cudaGetLastError());
+    p->launches++;
+    return MOC_OK;
+  }
   if (sizeof(T) == 4 && p->upd_items && p->ldg <= 128) {
     const size_t smem = sizeof(float) * ((size_t)d.n_groups * p->ldg +
                                          (size_t)UT_WARPS * d.n_groups * UT_ROWS);

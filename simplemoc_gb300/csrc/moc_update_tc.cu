@@ -1,0 +1,451 @@
+// update_sources (src/solver.c:1235-1320) of the MIXED mode on the tensor
+// cores: per tile of 128 fine regions of one material, one GEMM
+//
+//     D[r][n] = sum_k phi[r][k] * B[n][k],   B = [ S[m] ; nuSigmaF[m] ; SigmaA[m] ]
+//
+// on tcgen05 (kind::tf32, FP32 accumulation in tensor memory), so the scatter
+// source of every group, the fission rate and the absorption rate of a region
+// come out of the same product.  FP32 accuracy from TF32 operands by the
+// split-precision product x = hi + lo, hi = tf32(x):
+//     A.B ~ Ahi.Bhi + Ahi.Blo + Alo.Bhi         (three MMAs per K step)
+// whose dropped term Alo.Blo is ~2^-22 relative.  The tensor core rounds its
+// FP32 accumulation towards zero at each K step relative to the running sum, so
+// the main product Ahi.Bhi is accumulated in up to three K ranges, each in its
+// own tensor-memory accumulator, and the two correction products in a fourth;
+// the epilogue adds the four with FP32 round-to-nearest (the accumulation bias
+// drops from ~1.4e-6 to the level of the CUDA-core kernel).  The epilogue (one thread per
+// region row and half of its columns) forms the new source
+//     q = (nuSigmaF.phi / k * chi + S phi) / (4 pi)
+// with the residual and the k_eff partial sums, as update_tiled_kernel does.
+//
+// Shared-memory operands use the canonical K-major layout without swizzle:
+// 8-row x 16-byte core matrices, rows 16 bytes apart, core matrices along M/N
+// 128 bytes apart (the descriptor's stride offset) and along K `rows x 16`
+// bytes apart (its leading offset).  B is split and laid out once per upload on
+// the host; A is split while it is staged.
+#include <cstring>
+#include <vector>
+
+#include "moc_internal.h"
+
+namespace {
+
+constexpr int TC_M = 128;          // fine regions per tile = tensor-memory lanes
+constexpr int TC_THREADS = 256;    // two threads per region row
+constexpr int TC_MAX_KG = 26;      // K groups of 4 (groups <= 104)
+constexpr double TC_PI = 3.14159265358979323846;
+// ~1 s at 2 GHz: an MMA tile takes microseconds, so only a fault of the
+// tensor pipe runs this out
+constexpr long long TC_WAIT_CYCLES = 1LL << 31;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+// Shared-memory matrix descriptor: start address, leading (K) and stride
+// (M/N) byte offsets, descriptor version 1, no swizzle.
+__device__ __forceinline__ uint64_t mma_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = (uint64_t)((addr & 0x3FFFFu) >> 4);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1 << 46;
+  return d;
+}
+
+__device__ __forceinline__ float to_tf32(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return __uint_as_float(r);
+}
+
+__device__ __forceinline__ float4 ld_nc4(const float *p) {
+  float4 v;
+  asm("ld.global.nc.L1::no_allocate.v4.f32 {%0,%1,%2,%3}, [%4];"
+      : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+      : "l"(p));
+  return v;
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc,
+                                         uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(accumulate));
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t *bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_u32(bar))
+      : "memory");
+}
+
+// Waits for the barrier phase with a cycle limit; false when it ran out.
+__device__ __forceinline__ bool wait_phase(uint64_t *bar, uint32_t phase) {
+  const long long t0 = clock64();
+  for (;;) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred P1;\n\tmbarrier.try_wait.parity.shared::cta.b64 P1, [%1], %2;\n\t"
+        "selp.b32 %0, 1, 0, P1;\n\t}\n"
+        : "=r"(done)
+        : "r"(smem_u32(bar)), "r"(phase)
+        : "memory");
+    if (done) return true;
+    if (clock64() - t0 > TC_WAIT_CYCLES) return false;
+  }
+}
+
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+// 16 columns of the product: the main-product accumulators in K order, then
+// the corrections (at 3 * stride), added in FP32 round-to-nearest.  All loads
+// are issued before the one wait.
+__device__ __forceinline__ void tmem_ld16_nowait(uint32_t taddr, uint32_t (&r)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
+      "%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+}
+
+__device__ __forceinline__ void acc_ld16(uint32_t taddr, uint32_t stride, int n_chain,
+                                         float (&v)[16]) {
+  uint32_t ra[16], rb[16];
+  tmem_ld16_nowait(taddr, ra);                      // K range 0
+  if (n_chain > 1) tmem_ld16_nowait(taddr + stride, rb);   // K range 1
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i)
+    v[i] = n_chain > 1 ? __fadd_rn(__uint_as_float(ra[i]), __uint_as_float(rb[i]))
+                       : __uint_as_float(ra[i]);
+  if (n_chain > 2) tmem_ld16_nowait(taddr + 2 * stride, ra);   // K range 2
+  tmem_ld16_nowait(taddr + 3 * stride, rb);                    // corrections
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) {
+    if (n_chain > 2) v[i] = __fadd_rn(v[i], __uint_as_float(ra[i]));
+    v[i] = __fadd_rn(v[i], __uint_as_float(rb[i]));
+  }
+}
+
+__device__ __forceinline__ double block_sum_tc(double v, double *sh) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) sh[w] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (threadIdx.x == 0)
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) r += sh[i];
+  __syncthreads();
+  return r;   // valid in thread 0
+}
+
+struct TcArgs {
+  const float *phi;
+  float *q;
+  const int32_t *xs_order;
+  const int32_t *items;        // (material, first, end) in xs_order, <= 128 / F sources
+  int n_items;
+  const float *bmat;           // [n_xs][hi, lo][np * kp] in the canonical layout
+  const float *xs;             // [n_xs][G][3] (nuSigmaF, SigmaA, chi)
+  const double *scalars;
+  double *partials;
+  int32_t *err;
+  int n_partials;
+  int F, G, ldg, kp, np;
+  uint32_t acc_stride;         // tensor-memory columns per accumulator (power of 2 >= np)
+  uint32_t tmem_cols;          // 4 * acc_stride
+};
+
+// One thread's region row of a tile: material, the region (global row) and
+// whether the row exists (the last tile of a material is ragged).
+struct TileRow {
+  int m;
+  bool valid;
+  int64_t grow;
+};
+
+__device__ __forceinline__ TileRow tile_row(const TcArgs &x, int it, int row) {
+  TileRow t{0, false, 0};
+  if (it >= x.n_items) return t;
+  t.m = x.items[3 * it];
+  const int s0 = x.items[3 * it + 1], s1 = x.items[3 * it + 2];
+  t.valid = row < (s1 - s0) * x.F;
+  if (t.valid) t.grow = (int64_t)x.xs_order[s0 + row / x.F] * x.F + row % x.F;
+  return t;
+}
+
+// K groups j0 .. j1-1 of the row's fluxes, zero beyond G.
+__device__ __forceinline__ void load_fluxes(const TcArgs &x, const TileRow &t, int j0, int j1,
+                                            float4 (&buf)[(TC_MAX_KG + 1) / 2]) {
+  const float *prow = x.phi + t.grow * x.ldg;
+#pragma unroll
+  for (int i = 0; i < (TC_MAX_KG + 1) / 2; ++i) {
+    const int k = 4 * (j0 + i);
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (t.valid && j0 + i < j1 && k < x.ldg) v = ld_nc4(prow + k);
+    if (k + 0 >= x.G) v.x = 0.f;
+    if (k + 1 >= x.G) v.y = 0.f;
+    if (k + 2 >= x.G) v.z = 0.f;
+    if (k + 3 >= x.G) v.w = 0.f;
+    buf[i] = v;
+  }
+}
+
+__global__ void __launch_bounds__(TC_THREADS, 1) update_tc_kernel(TcArgs x) {
+  extern __shared__ __align__(128) float tc_smem[];
+  __shared__ __align__(8) uint64_t bar;
+  __shared__ uint32_t tmem_base;
+  __shared__ int abort_flag;
+  __shared__ double sh[TC_THREADS / 32];
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int row = tid & (TC_M - 1);            // = (warp % 4) * 32 + lane: its TMEM lane
+  const int half = tid >> 7;                   // 0: first half of the K groups / columns
+  const int KP = x.kp, NP = x.np, G = x.G, ldg = x.ldg;
+  float *a_hi = tc_smem;
+  float *a_lo = a_hi + TC_M * KP;
+  float *b_hi = a_lo + TC_M * KP;              // b_lo follows b_hi: one copy per material
+  float *b_lo = b_hi + NP * KP;
+  const int kgroups = KP / 4;
+  const int jh = (kgroups + 1) / 2;
+  const int j0 = half ? jh : 0, j1 = half ? kgroups : jh;
+
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(&tmem_base)),
+                 "r"(x.tmem_cols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(&bar)), "r"(1)
+                 : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    abort_flag = 0;
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_base;
+  const uint32_t taddr = tmem + ((uint32_t)((warp & 3) * 32) << 16);
+  const int ksteps = KP / 8;
+  const int n_chain = ksteps < 3 ? ksteps : 3;     // accumulators of the main product
+  const uint32_t AS = x.acc_stride;
+  // kind::tf32: F32 accumulator, TF32 A and B, both K-major, N = np, M = 128
+  const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(NP >> 3) << 17) |
+                         ((uint32_t)(TC_M >> 4) << 24);
+  const float inverse_k = (float)(1.0 / x.scalars[SC_KEFF_IN]);   // src/solver.c:1241
+  const float four_pi = (float)(4.0 * TC_PI);
+  const float r_four_pi = 1.0f / four_pi;
+  double res_acc = 0.0, abs_acc = 0.0, fis_acc = 0.0;
+  uint32_t phase = 0;
+  int cur_m = -1;
+
+  // Software pipeline over this block's tiles: while the tensor core works on
+  // tile i, the registers receive tile i+1's fluxes and tile i's old sources.
+  constexpr int HKG = (TC_MAX_KG + 1) / 2;      // K groups per thread
+  const int nch = (G + 15) / 16;                // 16-column chunks holding groups
+  const int ch_split = (nch + 1) / 2;
+  const int c0 = half ? ch_split : 0, c1 = half ? nch : ch_split;
+  float4 buf[HKG];
+  int it = blockIdx.x;
+  TileRow cur = tile_row(x, it, row);
+  load_fluxes(x, cur, j0, j1, buf);
+  while (it < x.n_items) {
+    if (cur.m != cur_m) {                       // the same on every thread
+      const uint4 *src = reinterpret_cast<const uint4 *>(x.bmat + (int64_t)cur.m * 2 * NP * KP);
+      uint4 *dst = reinterpret_cast<uint4 *>(b_hi);
+      for (int i = tid; i < 2 * NP * KP / 4; i += TC_THREADS) dst[i] = __ldg(src + i);
+      cur_m = cur.m;
+    }
+    // ---- A: this row's fluxes split into TF32 hi and lo (lo rounded as well:
+    // the tensor core would otherwise drop its low 13 bits, a bias to zero)
+#pragma unroll
+    for (int t = 0; t < HKG; ++t) {
+      const int j = j0 + t;
+      if (j >= j1) continue;
+      const float4 v = buf[t];
+      const float4 hi = make_float4(to_tf32(v.x), to_tf32(v.y), to_tf32(v.z), to_tf32(v.w));
+      const float4 lo = make_float4(to_tf32(v.x - hi.x), to_tf32(v.y - hi.y),
+                                    to_tf32(v.z - hi.z), to_tf32(v.w - hi.w));
+      const int off = j * (TC_M * 4) + row * 4;
+      *reinterpret_cast<float4 *>(a_hi + off) = hi;
+      *reinterpret_cast<float4 *>(a_lo + off) = lo;
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    // ---- the products, K steps of 8, issued by one thread
+    if (tid == 0) {
+      tc_fence_after();
+      const uint32_t lbo_a = TC_M * 16, lbo_b = (uint32_t)NP * 16;
+      const uint32_t ah = smem_u32(a_hi), al = smem_u32(a_lo);
+      const uint32_t bh = smem_u32(b_hi), bl = smem_u32(b_lo);
+      for (int kk = 0; kk < ksteps; ++kk) {
+        const uint64_t dah = mma_desc(ah + kk * 2 * lbo_a, lbo_a, 128);
+        const uint64_t dal = mma_desc(al + kk * 2 * lbo_a, lbo_a, 128);
+        const uint64_t dbh = mma_desc(bh + kk * 2 * lbo_b, lbo_b, 128);
+        const uint64_t dbl = mma_desc(bl + kk * 2 * lbo_b, lbo_b, 128);
+        const int chain = kk * n_chain / ksteps;
+        const bool first = kk == 0 || (kk - 1) * n_chain / ksteps != chain;
+        mma_tf32(tmem + (uint32_t)chain * AS, dah, dbh, idesc, first ? 0u : 1u);
+        mma_tf32(tmem + 3 * AS, dah, dbl, idesc, kk > 0 ? 1u : 0u);
+        mma_tf32(tmem + 3 * AS, dal, dbh, idesc, 1u);
+      }
+      mma_commit(&bar);
+    }
+    // ---- meanwhile: the next tile's fluxes and this tile's old sources
+    const int nx = it + (int)gridDim.x;
+    const TileRow nxt = tile_row(x, nx, row);
+    load_fluxes(x, nxt, j0, j1, buf);
+    float4 qold[16];
+#pragma unroll
+    for (int t = 0; t < 16; ++t) {
+      const int g = 16 * c0 + 4 * t;
+      qold[t] = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (cur.valid && g < 16 * c1 && g < ldg)
+        qold[t] = *reinterpret_cast<const float4 *>(x.q + cur.grow * ldg + g);
+    }
+    if (tid == 0) {
+      if (!wait_phase(&bar, phase)) {
+        abort_flag = 1;
+        atomicOr(x.err, 2);
+      }
+      tc_fence_before();
+    }
+    __syncthreads();
+    if (abort_flag) break;
+    phase ^= 1u;
+    tc_fence_after();
+    // ---- epilogue: fission and absorption columns G and G + 1, then the groups
+    float fis = 0.f, absr = 0.f;
+    {
+      float v[16];
+      acc_ld16(taddr + (uint32_t)(G & ~15), AS, n_chain, v);
+#pragma unroll
+      for (int e = 0; e < 16; ++e) {
+        if (e == (G & 15)) fis = v[e];
+        if (e == ((G + 1) & 15) && ((G + 1) & ~15) == (G & ~15)) absr = v[e];
+      }
+      if (((G + 1) & ~15) != (G & ~15)) {
+        acc_ld16(taddr + (uint32_t)((G + 1) & ~15), AS, n_chain, v);
+        absr = v[0];
+      }
+    }
+    const float fk = __fmul_rn(fis, inverse_k);
+    float res_row = 0.f;
+#pragma unroll
+    for (int cc = 0; cc < 4; ++cc) {            // this thread's chunks c0 .. c1-1
+      const int c = c0 + cc;
+      if (c >= c1) break;                       // the same on every lane of a warp
+      float v[16];
+      acc_ld16(taddr + (uint32_t)(16 * c), AS, n_chain, v);
+#pragma unroll
+      for (int qv = 0; qv < 4; ++qv) {
+        const int g = 16 * c + 4 * qv;
+        if (!cur.valid || g >= ldg) continue;
+        const float4 old = qold[4 * cc + qv];
+        float4 nw = old;
+        const float *po = &old.x;
+        float *pn = &nw.x;
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const int gg = g + e;
+          if (gg >= G) continue;
+          const float chi = __ldg(x.xs + ((int64_t)cur.m * G + gg) * 3 + 2);
+          // src/solver.c:1289-1295
+          const float num = __fadd_rn(__fmul_rn(fk, chi), v[4 * qv + e]);
+          float qq = __fmul_rn(num, r_four_pi);
+          qq = __fmaf_rn(__fmaf_rn(-qq, four_pi, num), r_four_pi, qq);
+          pn[e] = qq;
+          const float d = qq - po[e];
+          res_row += __fdividef(d * d, po[e] * po[e]);   // a diagnostic: fast quotient
+        }
+        *reinterpret_cast<float4 *>(x.q + cur.grow * ldg + g) = nw;
+      }
+    }
+    if (cur.valid) {
+      res_acc += (double)res_row;
+      if (half == 0) {
+        abs_acc += (double)absr;
+        fis_acc += (double)fis;
+      }
+    }
+    tc_fence_before();
+    __syncthreads();                            // TMEM read and A consumed: next tile
+    it = nx;
+    cur = nxt;
+  }
+  // ---- teardown: with the products drained, free the tensor memory
+  if (abort_flag && tid == 0) wait_phase(&bar, phase);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 0)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(x.tmem_cols)
+                 : "memory");
+  const double r = block_sum_tc(res_acc, sh);
+  if (tid == 0) x.partials[blockIdx.x] = r;
+  const double a = block_sum_tc(abs_acc, sh);
+  if (tid == 0) x.partials[x.n_partials + blockIdx.x] = a;
+  const double f = block_sum_tc(fis_acc, sh);
+  if (tid == 0) x.partials[2 * x.n_partials + blockIdx.x] = f;
+  if (blockIdx.x == 0)
+    for (int i = (int)gridDim.x + tid; i < x.n_partials; i += TC_THREADS)
+      x.partials[i] = x.partials[x.n_partials + i] = x.partials[2 * x.n_partials + i] = 0.0;
+}
+
+}  // namespace
+
+// Launches the tensor-core update (partials only; update_finalize follows).
+int moc_launch_update_tc(moc_problem *p) {
+  const int kp = p->tc_kp, np = p->tc_np;
+  if (!p->tc_b || kp == 0 || p->n_tc_items < 1) return MOC_ERR_UNSUPPORTED;
+  const size_t smem = sizeof(float) * (2 * (size_t)TC_M * kp + 2 * (size_t)np * kp);
+  // set outside any stream capture by the first call (the largest operands)
+  static bool attr_set = false;
+  if (!attr_set) {
+    const size_t max_smem =
+        sizeof(float) * (2 * (size_t)TC_M * 4 * TC_MAX_KG + 2 * (size_t)MOC_TC_MAX_NP * 4 * TC_MAX_KG);
+    MOC_CUDA_TRY(cudaFuncSetAttribute(update_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)max_smem));
+    attr_set = true;
+  }
+  int sms = 0;
+  MOC_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p->device));
+  TcArgs x{};
+  x.phi = p->phi;
+  x.q = p->q;
+  x.xs_order = p->xs_order;
+  x.items = p->tc_items;
+  x.n_items = p->n_tc_items;
+  x.bmat = p->tc_b;
+  x.xs = p->xs;
+  x.scalars = p->scalars;
+  x.partials = p->partials;
+  x.err = p->err;
+  x.n_partials = moc_post_scratch_blocks();
+  x.F = p->d.fai;
+  x.G = p->d.n_groups;
+  x.ldg = p->ldg;
+  x.kp = kp;
+  x.np = np;
+  x.acc_stride = 32;
+  while ((int)x.acc_stride < np) x.acc_stride <<= 1;
+  x.tmem_cols = 4 * x.acc_stride;                       // <= 512 (np <= 112)
+  int grid = sms < p->n_tc_items ? sms : p->n_tc_items;
+  if (grid > x.n_partials) grid = x.n_partials;
+  update_tc_kernel<<<grid, TC_THREADS, smem, p->stream>>>(x);
+  MOC_CUDA_TRY(cudaGetLastError());
+  p->launches++;
+  return MOC_OK;
+}

@@ -25,7 +25,7 @@ MODES = {"plain": L.MOC_MODE_PLAIN, "mixed": L.MOC_MODE_MIXED, "fp64": L.MOC_MOD
 
 class Solver:
     def __init__(self, problem: HostProblem, device: int = 0, mode: str = "plain",
-                 compensated: bool = False):
+                 compensated: bool = False, simt_update: bool = False):
         self._lib = L._lib()
         self.problem = problem
         self.spec = problem.spec
@@ -36,7 +36,7 @@ class Solver:
                                      C.byref(h)), "moc_create")
         self._h = h
         self.mode = "plain"
-        self.set_mode(mode, compensated)
+        self.set_mode(mode, compensated, simt_update)
 
     # ---- lifecycle ---------------------------------------------------------
     def close(self) -> None:
@@ -60,8 +60,12 @@ class Solver:
     def handle(self) -> C.c_void_p:
         return self._h
 
-    def set_mode(self, mode: str, compensated: bool = False) -> None:
-        flags = L.MOC_FLAG_COMPENSATED if compensated else 0
+    def set_mode(self, mode: str, compensated: bool = False, simt_update: bool = False) -> None:
+        """mode: "plain", "mixed" or "fp64".  compensated: MIXED tallies with
+        compensation.  simt_update: MIXED update_sources on the CUDA cores
+        instead of the tensor cores."""
+        flags = (L.MOC_FLAG_COMPENSATED if compensated else 0) | \
+            (L.MOC_FLAG_SIMT_UPDATE if simt_update else 0)
         L.check(self._lib.moc_set_mode(self._h, MODES[mode], flags), "moc_set_mode")
         self.mode = mode
 
