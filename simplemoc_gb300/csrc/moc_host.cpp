@@ -221,20 +221,19 @@ int moc_host_derive(const moc_dims *d, const moc_host *h, int32_t ldg, float *se
 void moc_host_coef(const moc_dims *d, const float *sigt, int32_t ldg, float *coef) {
   const int64_t G = d->n_groups;
   for (int64_t m = 0; m < d->n_sigt; m++) {
-    float *c = coef + m * 8 * (int64_t)ldg;
+    float *row = coef + m * MOC_COEF_PLANES * (int64_t)ldg;
     for (int64_t g = 0; g < ldg; g++) {
       const float sig = g < G ? sigt[m * G + g] : 1.0f;
       const float sig2 = sig * sig;                                        // src/solver.c:153
       const float sig3 = sig * sig2;                                       // src/solver.c:176
       const float sig4 = 3.f * sig2 * sig2;                                // src/solver.c:198
-      c[0 * ldg + g] = sig;
-      c[1 * ldg + g] = sig2;
-      c[2 * ldg + g] = sig3;
-      c[3 * ldg + g] = sig4;
-      c[4 * ldg + g] = 1.0f / sig;
-      c[5 * ldg + g] = 1.0f / sig2;
-      c[6 * ldg + g] = 1.0f / sig3;
-      c[7 * ldg + g] = 1.0f / sig4;
+      float *c = row + (g / 4) * 4 * MOC_COEF_PLANES + g % 4;
+      c[0] = sig;
+      c[4] = 1.0f / sig;
+      c[8] = 1.0f / sig2;
+      c[12] = 1.0f / sig3;
+      c[16] = 1.0f / sig4;
+      c[20] = 2.0f * (1.0f / sig3);
     }
   }
 }

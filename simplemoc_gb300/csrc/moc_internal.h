@@ -9,12 +9,10 @@
 
 #include "simplemoc_gb300.h"
 
-// Coefficients stored per (sigma_t row, group), as 8 planes of ldg floats:
-//   0 sigT   1 sigT^2   2 sigT*sigT^2   3 (3 sigT^2) sigT^2
-//   4..7 the correctly rounded float reciprocals of planes 0..3.
-// The products are formed in the reference's operand order
-// (src/solver.c:153,176,198) so they equal the reference's divisors bit for bit.
-enum { COEF_PLANES = 8 };
+#include "moc_host.h"
+
+// Coefficients per (sigma_t row, group): the interleaved planes of moc_host.h.
+enum { COEF_PLANES = MOC_COEF_PLANES };
 
 struct SweepArgs {
   const float *seg_ds;      // [N2D*P*S] 3D segment length per (2D track, polar, seg)

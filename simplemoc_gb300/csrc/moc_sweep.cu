@@ -80,8 +80,9 @@ __device__ __forceinline__ float table_lookup(const SweepArgs &a, const float2 *
 
 // 1 - exp(-tau) to ~1e-7 relative: Taylor series below 0.5, SFU exponential above.
 __device__ __forceinline__ float one_minus_exp(float t) {
-  float s = fmaf(t, -1.0f / 362880.0f, 1.0f / 40320.0f);
-  s = fmaf(t, s, -1.0f / 5040.0f);
+  // (1 - e^-t) / t = sum_k (-t)^k / (k+1)!, to degree 7: the first omitted
+  // term is t^8 / 9! <= 1.1e-8 below t = 0.5
+  float s = fmaf(t, 1.0f / 40320.0f, -1.0f / 5040.0f);
   s = fmaf(t, s, 1.0f / 720.0f);
   s = fmaf(t, s, -1.0f / 120.0f);
   s = fmaf(t, s, 1.0f / 24.0f);
@@ -183,24 +184,53 @@ __device__ __forceinline__ float plain_flat(const SweepArgs &a, const float2 *ta
 }
 
 // ---- MIXED arithmetic, quadratic source
-__device__ __forceinline__ float mixed_quad(const SweepArgs &a, float y1, float y2, float y3,
-                                            float sig, float r1, float r2, float r3, float r4,
-                                            float zin, float ds, float mu, float mu2, float w,
-                                            float &p) {
-  float c1 = (y1 - y3) * a.rd1;
-  float c2 = (fmaf(-2.f, y2, y1) + y3) * a.rd2;
-  float q0 = fmaf(fmaf(c2, zin, c1), zin, y2);
-  float q1 = fmaf(2.f * c2, zin, c1);
-  float tau = sig * ds;
-  float e = one_minus_exp(tau);
-  float reuse = fmaf(tau, tau - 2.f, 2.f * e * r3);
-  float A = fmaf(q0, tau, fmaf(sig, p, -q0) * e) * r2;
-  float q1mu = q1 * mu;
-  float q2mu2 = c2 * mu2;
-  float cub = fmaf(tau, fmaf(tau, tau - 3.f, 6.f), -6.f * e);
-  float fi = fmaf(q2mu2 * cub, r4, fmaf(q1mu, reuse, A));
-  float pn = fmaf(q0 * e, r1, fmaf(q1mu * (tau - e), r2, fmaf(q2mu2, reuse, p * (1.f - e))));
-  p = pn;
+// The fit q(z) = q0 + q1 (z - zin) + q2 (z - zin)^2 of the three fine sources
+// y1, y2, y3 (src/solver.c:69-81) with d1 = y1 - y3, d2 = y1 - 2 y2 + y3:
+//   q0 = y2 + d1 zin/(2dz) + d2 zin^2/(2dz^2),
+//   q1 mu = d1 mu/(2dz) + d2 (2 mu zin)/(2dz^2),   q2 mu^2 = d2 mu^2/(2dz^2).
+// The factors that depend only on the track (mu) and the segment (zin) are
+// formed once per segment (MixedFit), not once per group.
+struct MixedFit {
+  float a1, a0;        // zin/(2dz), zin^2/(2dz^2)
+  float b1, b2;        // mu/(2dz), 2 mu zin/(2dz^2)
+  float c2m;           // mu^2/(2dz^2)
+};
+
+__device__ __forceinline__ MixedFit mixed_fit(const SweepArgs &a, float zin, float mu,
+                                              float mu2) {
+  MixedFit f;
+  f.a1 = a.rd1 * zin;
+  f.a0 = a.rd2 * zin * zin;
+  f.b1 = mu * a.rd1;
+  f.b2 = 2.f * mu * a.rd2 * zin;
+  f.c2m = mu2 * a.rd2;
+  return f;
+}
+
+// The flux integral fi and the outgoing psi (src/solver.c:195-278) are both
+// linear in (q0, q1 mu, q2 mu^2, psi) with weights that depend on tau only:
+//   fi = q0 T + psi U + q1mu R + q2mu2 C/(3 sig^4)
+//   pn = q0 U + q1mu T + q2mu2 R + psi (1 - E)
+// with E = 1 - e^-tau, T = (tau - E)/sig^2, U = E/sig and the reference's
+// reuse term R = tau (tau - 2) + 2E/sig^3 (its precedence kept, as PLAIN).
+// r1, r2, r3x2, r4 are the coefficient planes 1/sig, 1/sig^2, 2/sig^3,
+// 1/(3 sig^4).
+__device__ __forceinline__ float mixed_quad(float y1, float y2, float y3, const MixedFit &f,
+                                            float sig, float r1, float r2, float r3x2,
+                                            float r4, float ds, float w, float &p) {
+  const float d1 = y1 - y3;
+  const float d2 = fmaf(-2.f, y2, y1) + y3;
+  const float q0 = fmaf(d2, f.a0, fmaf(d1, f.a1, y2));
+  const float q1mu = fmaf(d2, f.b2, d1 * f.b1);
+  const float q2mu2 = d2 * f.c2m;
+  const float tau = sig * ds;
+  const float E = one_minus_exp(tau);
+  const float T = (tau - E) * r2;
+  const float U = E * r1;
+  const float R = fmaf(E, r3x2, tau * (tau - 2.f));
+  const float Cr = fmaf(tau, fmaf(tau, tau - 3.f, 6.f), -6.f * E) * r4;
+  const float fi = fmaf(q0, T, fmaf(p, U, fmaf(q1mu, R, q2mu2 * Cr)));
+  p = fmaf(q0, U, fmaf(q1mu, T, fmaf(q2mu2, R, p * (1.f - E))));
   return w * fi;
 }
 
@@ -369,23 +399,24 @@ __device__ __forceinline__ void sweep_track(const SweepArgs &a, int64_t track, i
       load_rows<CPL, QUAD>(a, g1, li, TPW, rows1);
     }
     // ---- segment n
+    const MixedFit fit = (MODE == MODE_MIXED && QUAD) ? mixed_fit(a, g.zin, mu, mu2) : MixedFit{};
 #pragma unroll
     for (int k = 0; k < CPL; ++k) {
       const int c = li + TPW * k;
       if (c >= a.nchunk) continue;
       const int g4 = 4 * c;
-      const float *cf = a.coef + g.crow + g4;
+      const float *cf = a.coef + g.crow + 4 * COEF_PLANES * c;    // this chunk's planes
       const float4 sig = __ldg(reinterpret_cast<const float4 *>(cf));
-      const float4 r1 = __ldg(reinterpret_cast<const float4 *>(cf + 4 * a.ldg));
+      const float4 r1 = __ldg(reinterpret_cast<const float4 *>(cf + 4));
       float4 t;
       if (QUAD) {
         const float4 y1 = rows.v[k][0];
         const float4 y2 = rows.v[k][QUAD ? 1 : 0];
         const float4 y3 = rows.v[k][QUAD ? 2 : 0];
         if (MODE == MODE_PLAIN) {
-          const float4 r2 = __ldg(reinterpret_cast<const float4 *>(cf + 5 * a.ldg));
-          const float4 r3 = __ldg(reinterpret_cast<const float4 *>(cf + 6 * a.ldg));
-          const float4 r4 = __ldg(reinterpret_cast<const float4 *>(cf + 7 * a.ldg));
+          const float4 r2 = __ldg(reinterpret_cast<const float4 *>(cf + 8));
+          const float4 r3 = __ldg(reinterpret_cast<const float4 *>(cf + 12));
+          const float4 r4 = __ldg(reinterpret_cast<const float4 *>(cf + 16));
 #pragma unroll
           for (int e = 0; e < 4; ++e) {
             // the reference's divisors, formed with its own operations
@@ -400,14 +431,14 @@ __device__ __forceinline__ void sweep_track(const SweepArgs &a, int64_t track, i
             set(psi[k], e, p);
           }
         } else {
+          const float4 r2 = __ldg(reinterpret_cast<const float4 *>(cf + 8));
+          const float4 r4 = __ldg(reinterpret_cast<const float4 *>(cf + 16));
+          const float4 r3x2 = __ldg(reinterpret_cast<const float4 *>(cf + 20));
 #pragma unroll
           for (int e = 0; e < 4; ++e) {
-            const float q1r = get(r1, e);
-            const float q2r = q1r * q1r;
             float p = get(psi[k], e);
-            set(t, e, mixed_quad(a, get(y1, e), get(y2, e), get(y3, e), get(sig, e), q1r, q2r,
-                                 q1r * q2r, q2r * q2r * (1.0f / 3.0f), g.zin, ds, mu, mu2, w,
-                                 p));
+            set(t, e, mixed_quad(get(y1, e), get(y2, e), get(y3, e), fit, get(sig, e), get(r1, e),
+                                 get(r2, e), get(r3x2, e), get(r4, e), ds, w, p));
             set(psi[k], e, p);
           }
         }
@@ -548,7 +579,7 @@ __global__ void __launch_bounds__(BLOCK) sweep64_kernel(SweepArgs a) {
       double *fr = a.phi64 + (sb + fine) * a.ldg;
       const float *sigr = a.coef + (int64_t)__ldg(a.src_sigt + s) * COEF_PLANES * a.ldg;
       for (int g = li; g < a.G; g += TPW) {
-        const double sig = sigr[g];
+        const double sig = sigr[(g >> 2) * 4 * COEF_PLANES + (g & 3)];
         const double tau = sig * ds;
         const double e = -expm1(-tau);
         double p = a.psi64[tr * a.ldg + g];
@@ -990,7 +1021,7 @@ __device__ __forceinline__ AdjOut adj_flat(float y, float sig, float r1, float d
 // source rows and (reverse pass) dL/dphi of the tally row.
 template <int CPL, bool QUAD>
 struct AdjRows {
-  float4 sig[CPL], r1[CPL], y[CPL][QUAD ? 3 : 1], lam[CPL];
+  float4 sig[CPL], r1[CPL], r2[CPL], r3x2[CPL], r4[CPL], y[CPL][QUAD ? 3 : 1], lam[CPL];
 };
 
 template <int CPL, bool QUAD, bool LAM>
@@ -1000,9 +1031,14 @@ __device__ __forceinline__ void adj_load(const SweepArgs &a, const AdjArgs &x, c
   for (int k = 0; k < CPL; ++k) {
     const int c = li + TPW * k;
     if (c >= a.nchunk) continue;
-    const float *cf = a.coef + g.crow + 4 * c;
+    const float *cf = a.coef + g.crow + 4 * COEF_PLANES * c;
     r.sig[k] = __ldg(reinterpret_cast<const float4 *>(cf));
-    r.r1[k] = __ldg(reinterpret_cast<const float4 *>(cf + 4 * a.ldg));
+    r.r1[k] = __ldg(reinterpret_cast<const float4 *>(cf + 4));
+    if (!LAM && QUAD) {                 // the recomputation: the forward's planes
+      r.r2[k] = __ldg(reinterpret_cast<const float4 *>(cf + 8));
+      r.r4[k] = __ldg(reinterpret_cast<const float4 *>(cf + 16));
+      r.r3x2[k] = __ldg(reinterpret_cast<const float4 *>(cf + 20));
+    }
 const float *qr = a.q + g.qrow + 4 * c;
     r.y[k][0] = ld_stream(qr);
     if (QUAD) {
@@ -1096,6 +1132,7 @@ __global__ void __launch_bounds__(BLOCK, 2) adjoint_kernel(AdjArgs x) {
           s_ds[jj] = ds;
         }
         adj_load<CPL, QUAD, false>(a, x, g, li, TPW, cur);
+        const MixedFit fit = QUAD ? mixed_fit(a, g.zin, mu, mu2) : MixedFit{};
 #pragma unroll
         for (int k = 0; k < CPL; ++k) {
           hist_base[(jj * CPL + k) * BLOCK] = psi[k];
@@ -1104,13 +1141,13 @@ __global__ void __launch_bounds__(BLOCK, 2) adjoint_kernel(AdjArgs x) {
 #pragma unroll
           for (int e = 0; e < 4; ++e) {
             float p = get(psi[k], e);
-            const float q1r = get(cur.r1[k], e), q2r = q1r * q1r;
             if (QUAD)
-              mixed_quad(a, get(cur.y[k][0], e), get(cur.y[k][QUAD ? 1 : 0], e),
-                         get(cur.y[k][QUAD ? 2 : 0], e), get(cur.sig[k], e), q1r, q2r, q1r * q2r,
-                         q2r * q2r * (1.0f / 3.0f), g.zin, ds, mu, mu2, w, p);
+              mixed_quad(get(cur.y[k][0], e), get(cur.y[k][QUAD ? 1 : 0], e),
+                         get(cur.y[k][QUAD ? 2 : 0], e), fit, get(cur.sig[k], e),
+                         get(cur.r1[k], e), get(cur.r2[k], e), get(cur.r3x2[k], e),
+                         get(cur.r4[k], e), ds, w, p);
             else
-              mixed_flat(get(cur.y[k][0], e), get(cur.sig[k], e), q1r, ds, w_mu, p);
+              mixed_flat(get(cur.y[k][0], e), get(cur.sig[k], e), get(cur.r1[k], e), ds, w_mu, p);
             set(psi[k], e, p);
           }
         }
