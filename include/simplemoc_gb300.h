@@ -222,6 +222,23 @@ int moc_zero_state(moc_problem *p, int flux, int psi);
 int moc_get_fine_flux_device(moc_problem *p, float *phi);
 int moc_get_fine_flux64_device(moc_problem *p, double *phi);   /* FP64 mode */
 
+/* ---- OpenMOC track files (src/tracks.c:170-323, the reference's -d input) --
+ * moc_openmoc_probe reads the sizes of a track file; moc_openmoc_read fills
+ * caller arrays sized from them (any output may be NULL):
+ *   num_tracks, num_x, num_y, azim_weights  [n_azimuthal]
+ *   track_geometry [N2D][5] (x0, y0, x1, y1, phi), azim_index [N2D]
+ *   seg_off [N2D+1], seg_len / material_id / region_id [n_segments]
+ * Lengths are converted to float as the reference does.  cmfd != 0: the
+ * segments carry the two CMFD mesh-surface ids.  A missing, short or
+ * inconsistent file is MOC_ERR_ARG (the reference does not check). */
+int moc_openmoc_probe(const char *path, int cmfd, int32_t *n_azimuthal, double *spacing,
+                      int64_t *n_tracks_2d, int64_t *n_segments);
+int moc_openmoc_read(const char *path, int cmfd, int64_t n_tracks_2d, int64_t n_segments,
+                     int32_t *num_tracks, int32_t *num_x, int32_t *num_y,
+                     double *azim_weights, double *track_geometry, int32_t *azim_index,
+                     int64_t *seg_off, float *seg_len, int32_t *material_id,
+                     int32_t *region_id);
+
 /* ---- adjoint sweep (no counterpart in the reference) ------------------- */
 /* Reverse-mode derivative of one transport sweep in the MIXED arithmetic
  * (the PLAIN table is piecewise linear with jumps, not differentiable).

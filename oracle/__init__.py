@@ -278,6 +278,29 @@ class Reference:
         finally:
             self.lib.refh_teardown()
 
+    def load_openmoc(self, path, cmfd: bool = False, cap_tracks: int = 1 << 16,
+                     cap_segs: int = 1 << 22) -> dict:
+        """The reference's own load_OpenMOC_tracks on `path`: per 2D track its
+        segment count, per segment the float length and region id, and the
+        reader's metadata (n_azimuthal, radial_ray_sep, segments_per_track)."""
+        fn = self.lib.refh_load_openmoc
+        fn.restype = C.c_long
+        fn.argtypes = [C.c_char_p, C.c_int, C.c_long, C.c_long, C.POINTER(C.c_int),
+                       C.POINTER(C.c_float), C.POINTER(C.c_long), C.c_void_p, C.c_void_p,
+                       C.c_void_p]
+        nseg = np.zeros(cap_tracks, np.int64)
+        lens = np.zeros(cap_segs, np.float32)
+        ids = np.zeros(cap_segs, np.int64)
+        n_az, sep, spt = C.c_int(), C.c_float(), C.c_long()
+        n = fn(str(path).encode(), int(cmfd), cap_tracks, cap_segs, C.byref(n_az), C.byref(sep),
+               C.byref(spt), nseg.ctypes.data, lens.ctypes.data, ids.ctypes.data)
+        if n < 0:
+            raise ValueError("track file larger than the harness buffers")
+        m = int(nseg[:n].sum())
+        return {"n_tracks_2d": int(n), "n_segments": nseg[:n].copy(), "lengths": lens[:m].copy(),
+                "source_ids": ids[:m].copy(), "n_azimuthal": n_az.value,
+                "radial_ray_sep": sep.value, "segments_per_track": spt.value}
+
     def iterate(self, hp, state: dict, n_iters: int, keff: float = 1.0, sweep_only=False):
         op = make_problem(hp)
         f = C.c_float

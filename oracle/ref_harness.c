@@ -13,6 +13,7 @@
  *   update_sources                           (src/solver.c:1235)
  *   compute_keff                             (src/solver.c:1324)
  *   buildExponentialTable                    (src/utils.c:48)
+ *   load_OpenMOC_tracks                      (src/tracks.c:170)
  * The only restated part is the traversal: the reference draws the source
  * region of each 3D segment from a time-seeded rand_r (src/solver.c:476-483)
  * and splits 2D segments axially; here every 3D track walks its explicit
@@ -228,4 +229,37 @@ float refh_compute_keff(void)
   CommGrid grid;
   memset(&grid, 0, sizeof grid);
   return compute_keff(Pr, I, grid);
+}
+
+/* The reference's own OpenMOC track-file reader (src/tracks.c:170-323):
+ * loads `path` and copies out what the traversal uses (per 2D track its
+ * segment count, per segment its float length and region id), with the
+ * reader's metadata.  Returns the number of 2D tracks, or -1 when the caller's
+ * arrays (cap_tracks, cap_segs) are too small. */
+long refh_load_openmoc(const char *path, int cmfd, long cap_tracks, long cap_segs,
+                       int *n_azimuthal, float *ray_sep, long *segments_per_track,
+                       long *n_segments, float *lengths, long *source_ids)
+{
+  Input in;
+  memset(&in, 0, sizeof in);
+  in.n_polar_angles = 1;
+  in.z_stacked = 1;
+  size_t nbytes = 0;
+  Track2D *t = load_OpenMOC_tracks((char *)path, cmfd != 0, &in, &nbytes);
+  long n = in.ntracks_2D, k = 0;
+  if (n > cap_tracks) n = -1;
+  for (long i = 0; n >= 0 && i < n; i++) {
+    n_segments[i] = t[i].n_segments;
+    for (long s = 0; s < t[i].n_segments; s++, k++) {
+      if (k >= cap_segs) { n = -1; break; }
+      lengths[k] = t[i].segments[s].length;
+      source_ids[k] = t[i].segments[s].source_id;
+    }
+  }
+  *n_azimuthal = in.n_azimuthal;
+  *ray_sep = in.radial_ray_sep;
+  *segments_per_track = in.segments_per_track;
+  if (in.ntracks_2D > 0) free(t[0].segments);      /* the loader's contiguous block */
+  free(t);
+  return n;
 }

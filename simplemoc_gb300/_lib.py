@@ -110,6 +110,12 @@ SIGNATURES = {
     "moc_adjoint_backward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                        C.c_void_p]),
     "moc_set_adjoint_width": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "moc_openmoc_probe": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(C.c_int32),
+                                    C.POINTER(C.c_double), C.POINTER(C.c_int64),
+                                    C.POINTER(C.c_int64)]),
+    "moc_openmoc_read": (C.c_int, [C.c_char_p, C.c_int, C.c_int64, C.c_int64, C.c_void_p,
+                                   C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                   C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "moc_batch_create": (C.c_int, [C.c_int, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p)]),
     "moc_batch_destroy": (C.c_int, [C.c_void_p]),
     "moc_batch_autotune": (C.c_int, [C.c_void_p]),

@@ -26,7 +26,7 @@ ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 CU_SOURCES = ["moc_api.cu", "moc_sweep.cu", "moc_post.cu", "moc_refabi.cu", "moc_batch.cu",
               "moc_update_tc.cu"]
-CPP_SOURCES = ["moc_host.cpp"]
+CPP_SOURCES = ["moc_host.cpp", "moc_openmoc.cpp"]
 
 
 def _nvcc() -> str:

@@ -129,3 +129,38 @@ def test_dropin_reports_bad_axial_order_without_exiting(ref_lib):
     ref_lib.transport_sweep(C.byref(rp.params), C.byref(rp.input))
     assert ref_lib.moc_ref_status() == 1
     assert rp.input.segments_processed == -7
+
+
+def test_dropin_sweep_of_an_openmoc_track_file(ref_lib, port, tmp_path):
+    """A track file (src/tracks.c:170-323) read by the library's reader and
+    swept by the drop-in traversal equals the oracle's traversal of the same
+    2D tracks: psi, heights and sub-segment counts bit for bit."""
+    import simplemoc_gb300 as sm
+    from simplemoc_gb300 import openmoc, refabi
+    t, len64 = openmoc.synthetic(12, n_azimuthal=4, tracks_per_angle=2, segments_per_track=30)
+    path = tmp_path / "tracks.bin"
+    openmoc.write(path, t, seg_len64=len64)
+    tr = openmoc.read(path)
+    height, sep, n_polar = 40.0, 0.5, 4
+    z_stacked = int(height / sep)
+    spec = sm.ProblemSpec(n_groups=24, fai=5, cai=4, height=height, n_sources=80,
+                          n_tracks_2d=tr.n_tracks_2d, n_polar=n_polar, z_stacked=z_stacked,
+                          n_seg=10, seed=41)
+    hp = sm.generate(spec)
+    geo = openmoc.to_geometry(tr, n_polar, z_stacked, sep, seed=5)
+    rp = refabi.build(hp, geo)
+    rg = oracle.make_refgeo(geo)
+    op = oracle.make_problem(hp)
+    st = oracle.fresh_state(hp)
+    z = geo.z_height.copy()
+    for sweep in range(2):
+        LIBC.srand(70 + sweep)
+        ref_lib.transport_sweep(C.byref(rp.params), C.byref(rp.input))
+        assert ref_lib.moc_ref_status() == 0
+        LIBC.srand(70 + sweep)
+        n = port.ref_sweep(op, rg, st["fine_source"], st["fine_flux"], st["psi_f"], z)
+        assert rp.input.segments_processed == n
+        assert ref_lib.moc_ref_sync_to_host(C.byref(rp.params), C.byref(rp.input)) == 0
+        assert np.array_equal(rp.z_heights(), z)
+        assert np.array_equal(rp.psi_f, st["psi_f"])
+        assert rel_err(rp.fine_flux, st["fine_flux"]) <= 1e-5
