@@ -426,21 +426,24 @@ def main():
     e2e = None
     if e2e_on:
         out = {"fine_flux": alloc((spec.n_fsr * spec.n_groups,), np.float32)}
-        steps = min(K, 3)
+        steps = min(K, 5)
         solver.upload(hp)
         solver.power_iteration(1.0)
         solver.download(fine_flux=True, fine_source=False, psi_f=False, out=out)
         barrier()
         t0 = time.perf_counter()
+        marks = [t0]
         for _ in range(steps):
             solver.upload(hp)
             solver.power_iteration(1.0)
             solver.download(fine_flux=True, fine_source=False, psi_f=False, out=out)
-        dt = time.perf_counter() - t0
+            marks.append(time.perf_counter())
+        dt = marks[-1] - t0
         barrier()
         e2e = {"value": world * ints * steps / dt, "unit": "integrations/s",
                "h2d_bytes_per_step": hp.input_nbytes(),
-               "d2h_bytes_per_step": int(out["fine_flux"].nbytes + 16)}
+               "d2h_bytes_per_step": int(out["fine_flux"].nbytes + 16),
+               "ms_steps": [round(1e3 * (b - a), 2) for a, b in zip(marks, marks[1:])]}
 
     # ---- accuracy of the chosen mode against FP64 on a reduced problem ---------
     accuracy = None
