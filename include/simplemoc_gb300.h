@@ -148,7 +148,10 @@ int moc_destroy(moc_problem *p);
  * chunk as soon as it lands, and every other call waits for the copies first.
  * The host arrays must stay unchanged until a call that waits for the device
  * (moc_synchronize, moc_download, moc_power_iteration with outputs, ...) has
- * returned.  Invalid source ids are rejected here (MOC_ERR_ARG). */
+ * returned.  The host validates the input while the copies run; invalid input
+ * (e.g. a source id out of range) is MOC_ERR_ARG, after the call has let its
+ * copies finish, and then every other call returns MOC_ERR_STATE until an
+ * upload succeeds (the device state is partly overwritten). */
 int moc_upload(moc_problem *p, const moc_host *host);
 /* Copies results back (any pointer may be NULL to skip that array). */
 int moc_download(moc_problem *p, float *fine_flux, float *fine_source,
@@ -169,6 +172,12 @@ int moc_set_mode(moc_problem *p, int mode, int flags);
 int moc_set_launch(moc_problem *p, int threads_per_track, int chunks_per_thread);
 int moc_get_launch(const moc_problem *p, int *threads_per_track,
                    int *chunks_per_thread);
+/* The sweep's pipeline: 0 prefetches the next segment's fine-source rows into
+ * registers; 4 copies them into a 4-stage shared-memory ring per track with
+ * the bulk-copy engine, 3 segments ahead (MIXED and PLAIN, explicit streams);
+ * -1 = automatic (moc_autotune times both). */
+int moc_set_pipeline(moc_problem *p, int stages);
+int moc_get_pipeline(const moc_problem *p, int *stages);
 
 /* Autotuner: times every launch shape of the current mode on the first
  * n_tracks tracks (0 = up to 262144), with scratch tally and angular-flux

@@ -103,6 +103,20 @@ int upload_all(moc_problem *p, const moc_host *h, bool stream_tracks) {
   const moc_dims &d = p->d;
   const int64_t N2D = d.n_tracks_2d, P = d.n_polar, S = d.n_seg, G = d.n_groups;
   const int64_t NS = d.n_sources;
+  if (stream_tracks) {
+    // Fine source and flux (2 GB on the default problem) go first, so that the
+    // host's validation and derivation below run while they are in flight; the
+    // per-track arrays follow on the copy stream at the end.  The copy stream
+    // waits for the work already queued on the stream (a sweep may still read
+    // the arrays it overwrites).  The arrays copied before the validation must
+    // at least exist.
+    if (!h->fine_source || !h->seg_src) return MOC_ERR_ARG;
+    MOC_CUDA_TRY(cudaEventRecord(p->main_ev, p->stream));
+    MOC_CUDA_TRY(cudaStreamWaitEvent(p->copy_stream, p->main_ev, 0));
+    TRY(put_rows(p, p->q, h->fine_source, p->nfsr));
+    TRY(put_rows(p, p->phi, h->fine_flux, p->nfsr));
+    TRY(moc_host_validate(&d, h));
+  }
   std::vector<float> seg_ds((size_t)(N2D * P * S)), mu((size_t)P), weight((size_t)p->n3d);
   std::vector<float> coef((size_t)d.n_sigt * COEF_PLANES * p->ldg);
   std::vector<float> st((size_t)d.n_xs * G * G);
@@ -192,13 +206,15 @@ int upload_all(moc_problem *p, const moc_host *h, bool stream_tracks) {
     // the pageable sources above must be consumed before the vectors go away
     MOC_CUDA_TRY(cudaStreamSynchronize(p->stream));
   }
-  TRY(put_rows(p, p->q, h->fine_source, p->nfsr));
-  TRY(put_rows(p, p->phi, h->fine_flux, p->nfsr));
-  if (stream_tracks) {
-    // the copies wait for the work already queued on the stream (a sweep may
-    // still read the arrays they overwrite)
-    MOC_CUDA_TRY(cudaEventRecord(p->main_ev, p->stream));
-    MOC_CUDA_TRY(cudaStreamWaitEvent(p->copy_stream, p->main_ev, 0));
+  if (!stream_tracks) {
+    TRY(put_rows(p, p->q, h->fine_source, p->nfsr));
+    TRY(put_rows(p, p->phi, h->fine_flux, p->nfsr));
+    TRY(put(p, p->seg_src, h->seg_src, p->n3d * S));
+    TRY(put_rows(p, p->psi_f, h->psi_f, p->n3d));
+    TRY(put_rows(p, p->psi_b, h->psi_b, p->n3d));
+  } else {
+    // the per-track arrays last: the host-to-device copies run in issue order,
+    // and the small arrays above are what the first chunk's sweep waits for
     const int n = (int)(N2D < moc_problem::MAX_UPLOAD_CHUNKS ? N2D : moc_problem::MAX_UPLOAD_CHUNKS);
     const int64_t PZ = P * d.z_stacked;
     for (int k = 0; k < n; ++k) {
@@ -213,10 +229,6 @@ int upload_all(moc_problem *p, const moc_host *h, bool stream_tracks) {
     TRY(put_rows(p, p->psi_b, h->psi_b, p->n3d, p->copy_stream));
     MOC_CUDA_TRY(cudaEventRecord(p->copy_done, p->copy_stream));
     p->n_chunks = n;
-  } else {
-    TRY(put(p, p->seg_src, h->seg_src, p->n3d * S));
-    TRY(put_rows(p, p->psi_f, h->psi_f, p->n3d));
-    TRY(put_rows(p, p->psi_b, h->psi_b, p->n3d));
   }
   if (p->phi_lo)
     MOC_CUDA_TRY(cudaMemsetAsync(p->phi_lo, 0, sizeof(float) * (size_t)(p->nfsr * p->ldg), p->stream));
@@ -270,6 +282,7 @@ int fail(moc_problem *p, int rc) {
 int usable(const moc_problem *p) {
   if (!p) return MOC_ERR_ARG;
   if (p->status != MOC_OK) return MOC_ERR_STATE;
+  if (p->stale) return MOC_ERR_STATE;      // a rejected upload: upload again
   return MOC_OK;
 }
 
@@ -449,15 +462,32 @@ int moc_destroy(moc_problem *p) {
 }
 
 int moc_upload(moc_problem *p, const moc_host *host) {
-  int rc = ready(p);
-  if (rc != MOC_OK) return rc;
+  if (!p) return MOC_ERR_ARG;
+  if (p->status != MOC_OK) return MOC_ERR_STATE;
   if (!host) return MOC_ERR_ARG;
-  rc = moc_host_validate(&p->d, host);
-  if (rc != MOC_OK) return rc;
-  // FP64 state is widened from the uploaded FP32 state at once: no streaming
-  rc = upload_all(p, host, p->q64 == nullptr);
+  cudaSetDevice(p->device);
+  int rc = moc_join_upload(p);
   if (rc != MOC_OK) return fail(p, rc);
-  return MOC_OK;
+  // FP64 state is widened from the uploaded FP32 state at once: no streaming.
+  // Streamed uploads validate while their copies are in flight.
+  const bool streamed = p->q64 == nullptr;
+  if (!streamed) {
+    rc = moc_host_validate(&p->d, host);
+    if (rc != MOC_OK) return rc;
+  }
+  rc = upload_all(p, host, streamed);
+  if (rc == MOC_OK) {
+    p->stale = false;
+    return MOC_OK;
+  }
+  // a rejected input after copies were issued: let them finish (the caller
+  // may free its buffers) and refuse work until a valid upload
+  cudaStreamSynchronize(p->copy_stream);
+  cudaStreamSynchronize(p->stream);
+  p->n_chunks = 0;
+  p->detect_pending = false;
+  p->stale = true;
+  return rc == MOC_ERR_ARG ? rc : fail(p, rc);
 }
 
 int moc_download(moc_problem *p, float *fine_flux, float *fine_source, float *psi_f, float *psi_b) {
@@ -554,6 +584,19 @@ int moc_set_launch(moc_problem *p, int threads_per_track, int chunks_per_thread)
   return MOC_ERR_UNSUPPORTED;
 }
 
+int moc_set_pipeline(moc_problem *p, int stages) {
+  if (!p) return MOC_ERR_ARG;
+  if (stages != -1 && stages != 0 && stages != 4) return MOC_ERR_UNSUPPORTED;
+  p->stages = stages;
+  return MOC_OK;
+}
+
+int moc_get_pipeline(const moc_problem *p, int *stages) {
+  if (!p || !stages) return MOC_ERR_ARG;
+  *stages = p->stages > 0 ? p->stages : 0;
+  return MOC_OK;
+}
+
 int moc_set_adjoint_width(moc_problem *p, int lanes_per_track, int chunks_per_lane) {
   if (!p) return MOC_ERR_ARG;
   if (lanes_per_track == 0 && chunks_per_lane == 0) {
@@ -578,11 +621,12 @@ int moc_autotune(moc_problem *p, int64_t n_tracks, int *threads_per_track,
   int rc = ready(p);
   if (rc != MOC_OK) return rc;
   cudaSetDevice(p->device);
-  int tpw = 0, cpl = 0;
-  rc = moc_sweep_autotune(p, n_tracks, &tpw, &cpl, ms_best);
+  int tpw = 0, cpl = 0, stages = 0;
+  rc = moc_sweep_autotune(p, n_tracks, &tpw, &cpl, &stages, ms_best);
   if (rc != MOC_OK) return rc;
   p->tpw = tpw;
   p->cpl = cpl;
+  p->stages = stages;
   if (threads_per_track) *threads_per_track = tpw;
   if (chunks_per_thread) *chunks_per_thread = cpl;
   return MOC_OK;

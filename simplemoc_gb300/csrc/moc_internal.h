@@ -63,6 +63,8 @@ struct moc_problem {
   int mode = MOC_MODE_PLAIN;
   int flags = 0;
   int tpw = 0, cpl = 0;          // 0 = automatic
+  int stages = -1;               // sweep pipeline: 0 register prefetch, N > 0 an N-stage
+                                 // shared-memory ring; -1 = automatic (0 until tuned)
   int adj_tpw = 0, adj_cpl = 0;  // reverse sweep lanes per track, chunks per lane; 0 = automatic
   int64_t launches = 0;
   int64_t n3d = 0, nfsr = 0;
@@ -119,6 +121,7 @@ struct moc_problem {
   int64_t chunk_end[MAX_UPLOAD_CHUNKS] = {};     // one past the chunk's last 2D track
   int n_chunks = 0;
   bool detect_pending = false;                   // psi_b's nonzero flag still to be set
+  bool stale = false;                            // an upload was rejected: device state undefined
   // host copies needed for re-upload and derived arrays
   float polar[64];
 };
@@ -168,7 +171,8 @@ int moc_launch_sweep_ckpt(moc_problem *p, float *ck_psi, float *ck_z, int k, int
 int moc_launch_adjoint(moc_problem *p, const float *ck_psi, const float *ck_z, int k, int nck,
                        const float *dphi, float *dq, double *dsig, float *dpsi_in);
 int moc_sweep_launch_shape(const moc_problem *p, int *tpw, int *cpl);
-int moc_sweep_autotune(moc_problem *p, int64_t n_sub, int *tpw, int *cpl, double *ms);
+int moc_sweep_autotune(moc_problem *p, int64_t n_sub, int *tpw, int *cpl, int *stages,
+                       double *ms);
 int moc_launch_renormalize(moc_problem *p);
 int moc_launch_update(moc_problem *p, double keff, bool keff_on_device, bool with_keff);
 int moc_set_leakage(moc_problem *p, double leakage);

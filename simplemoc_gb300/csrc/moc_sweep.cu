@@ -498,6 +498,281 @@ __global__ void __launch_bounds__(BLOCK) sweep_kernel(SweepArgs a) {
     sweep_track<TPW, CPL, MODE, QUAD, CSR, CKPT>(a, base + gw, lane, TPW, s_table);
 }
 
+// ---- Staged sweep.  The fine-source rows of each segment (the three fit rows
+// are one contiguous block, 16-byte aligned) are copied into a ring of NST
+// shared-memory stages per track by the bulk-copy engine (cp.async.bulk with
+// mbarrier::complete_tx), NST-1 segments ahead of the arithmetic, so the bytes
+// in flight cost no registers.  The track's lanes run the geometry ahead (the
+// height chain runs NST-1 segments ahead of the arithmetic); lane 0 stores it
+// beside the stage and issues the copy.  The lanes wait on the stage's barrier
+// (bounded), read the rows from shared memory and do the arithmetic and the
+// tallies of sweep_track.  Every wait has a cycle limit; on expiry the kernel
+// sets error bit 2, lets its copies in flight land (bounded) and returns.
+constexpr long long STAGE_WAIT_CYCLES = 1LL << 31;     // ~1 s at 2 GHz
+
+struct StageGeo {              // 32 bytes, beside each stage
+  float zin, ds;
+  int mat, pad;
+  int64_t frow, crow;
+};
+
+__device__ __forceinline__ uint32_t smem_addr(const void *p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ bool stage_wait(uint64_t *bar, uint32_t phase) {
+  const long long t0 = clock64();
+  for (;;) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred P1;\n\tmbarrier.try_wait.parity.shared::cta.b64 P1, [%1], %2;\n\t"
+        "selp.b32 %0, 1, 0, P1;\n\t}\n"
+        : "=r"(done)
+        : "r"(smem_addr(bar)), "r"(phase)
+        : "memory");
+    if (done) return true;
+    if (clock64() - t0 > STAGE_WAIT_CYCLES) return false;
+  }
+}
+
+__device__ __forceinline__ void stage_issue(uint64_t *bar, void *dst, const void *src,
+                                            uint32_t bytes) {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+               "r"(bytes)
+               : "memory");
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+          "r"(smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+
+// Per-track state of the copy side or the arithmetic side: the track, its
+// polar cosine, and the segment cursor.
+struct StageCursor {
+  int64_t base;          // the warp's current track base (tracks base + gw)
+  int64_t tr;            // this group's track (clamped), valid if < n3d
+  bool valid;
+  int seg;               // next segment
+  float mu;
+};
+
+__device__ __forceinline__ void cursor_track(const SweepArgs &a, StageCursor &c, int gw) {
+  const int64_t track = c.base + gw;
+  c.valid = track < a.n3d;
+  c.tr = c.valid ? track : a.n3d - 1;
+  c.mu = a.mu[(int)((c.tr / a.Z) % a.P)];
+  c.seg = 0;
+}
+
+template <int TPW, int CPL, int MODE, bool QUAD, int NST>
+__global__ void __launch_bounds__(BLOCK) sweep_staged_kernel(SweepArgs a, int rowbytes) {
+  extern __shared__ __align__(128) unsigned char s_dyn[];
+  constexpr int GPW = 32 / TPW;
+  constexpr int GROUPS = BLOCK / TPW;
+  // [table (PLAIN)] [barriers] [geometry] [rows], each region 128-byte aligned
+  const int tab_bytes = MODE == MODE_PLAIN ? ((int)sizeof(float2) * a.table_n + 127) / 128 * 128 : 0;
+  float2 *s_table = reinterpret_cast<float2 *>(s_dyn);
+  uint64_t *s_bar = reinterpret_cast<uint64_t *>(s_dyn + tab_bytes);
+  StageGeo *s_geo = reinterpret_cast<StageGeo *>(s_dyn + tab_bytes + ((GROUPS * NST * 8 + 127) / 128) * 128);
+  unsigned char *s_rows = reinterpret_cast<unsigned char *>(s_geo) +
+                          ((GROUPS * NST * (int)sizeof(StageGeo) + 127) / 128) * 128;
+  const int lane = threadIdx.x & 31;
+  const int li = lane % TPW;
+  const int gw = lane / TPW;
+  const int grp = (threadIdx.x >> 5) * GPW + gw;
+  uint64_t *bar = s_bar + grp * NST;
+  StageGeo *geo = s_geo + grp * NST;
+  unsigned char *rows = s_rows + (size_t)grp * NST * rowbytes;
+  if (MODE == MODE_PLAIN)
+    for (int i = threadIdx.x; i < a.table_n; i += BLOCK) s_table[i] = a.table[i];
+  if (li == 0)
+    for (int k = 0; k < NST; ++k)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar + k)), "r"(1)
+                   : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  __syncthreads();
+
+  const int64_t warp_id = ((int64_t)blockIdx.x * BLOCK + threadIdx.x) >> 5;
+  const int64_t stride = (((int64_t)gridDim.x * BLOCK) >> 5) * GPW;
+  const int S = a.S;
+  const int64_t PZ = (int64_t)a.P * a.Z;
+
+  // ---- copy side: cursor, height chain and segment-stream chunks
+  StageCursor pc;
+  pc.base = warp_id * GPW;
+  cursor_track(a, pc, gw);
+  float pz = a.z0[pc.tr];
+  const float *p_dsb = a.seg_ds + (pc.tr / PZ * a.P + (int)((pc.tr / a.Z) % a.P)) * S;
+  const int32_t *p_srcb = a.seg_src + pc.tr * S;
+  float ds_c = li < S ? __ldg(p_dsb + li) : 0.f;
+  int src_c = li < S ? __ldg(p_srcb + li) : 0;
+  float ds_n = TPW + li < S ? __ldg(p_dsb + TPW + li) : 0.f;
+  int src_n = TPW + li < S ? __ldg(p_srcb + TPW + li) : 0;
+  uint32_t issued = 0, consumed = 0;
+  bool abort = false;
+
+  // issues the copy of the copy cursor's segment; all lanes of the warp call it
+  auto issue = [&]() {
+    const int k = pc.seg % TPW;
+    if (k == 0 && pc.seg > 0) {
+      ds_c = ds_n;
+      src_c = src_n;
+      const int nl = pc.seg + TPW + li;
+      ds_n = nl < S ? __ldg(p_dsb + nl) : 0.f;
+      src_n = nl < S ? __ldg(p_srcb + nl) : 0;
+    }
+    const float ds = __shfl_sync(FULL, ds_c, k, TPW);
+    const int src = __shfl_sync(FULL, src_c, k, TPW);
+    const Seg g = segment_geometry(a, pz, checked_source(a, src, li));
+    const int slot = (int)(issued % NST);
+    if (li == 0) {
+      StageGeo sg;
+      sg.zin = g.zin;
+      sg.ds = ds;
+      sg.mat = g.mat;
+      sg.pad = 0;
+      sg.frow = g.frow;
+      sg.crow = g.crow;
+      geo[slot] = sg;
+      stage_issue(bar + slot, rows + (size_t)slot * rowbytes, a.q + g.qrow, (uint32_t)rowbytes);
+    }
+    ++issued;
+    pz = advance_z(a, pz, ds, pc.mu);
+    if (++pc.seg == S) {                       // the next track of this group
+      pc.base += stride;
+      cursor_track(a, pc, gw);
+      pz = a.z0[pc.tr];
+      p_dsb = a.seg_ds + (pc.tr / PZ * a.P + (int)((pc.tr / a.Z) % a.P)) * S;
+      p_srcb = a.seg_src + pc.tr * S;
+      ds_c = li < S ? __ldg(p_dsb + li) : 0.f;
+      src_c = li < S ? __ldg(p_srcb + li) : 0;
+      ds_n = TPW + li < S ? __ldg(p_dsb + TPW + li) : 0.f;
+      src_n = TPW + li < S ? __ldg(p_srcb + TPW + li) : 0;
+    }
+  };
+
+  for (int k = 0; k < NST && pc.base < a.n3d; ++k) issue();
+
+  // ---- arithmetic side: one track after the other
+  for (int64_t base = warp_id * GPW; base < a.n3d && !abort; base += stride) {
+    const int64_t track = base + gw;
+    const bool valid = track < a.n3d;
+    const int64_t tr = valid ? track : a.n3d - 1;
+    const float mu = a.mu[(int)((tr / a.Z) % a.P)];
+    const float mu2 = __fmul_rn(mu, mu);          // as sweep_track: the same psi
+    const float w = a.weight[tr];
+    const float w_mu = __fmul_rn(w, mu);
+    float4 psi[CPL];
+#pragma unroll
+    for (int k = 0; k < CPL; ++k) {
+      const int c = li + TPW * k;
+      psi[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (c < a.nchunk) psi[k] = *reinterpret_cast<const float4 *>(a.psi + tr * a.ldg + 4 * c);
+      if (a.psi_scale) {
+        const float sc = *a.psi_scale;
+        psi[k].x = __fmul_rn(psi[k].x, sc);
+        psi[k].y = __fmul_rn(psi[k].y, sc);
+        psi[k].z = __fmul_rn(psi[k].z, sc);
+        psi[k].w = __fmul_rn(psi[k].w, sc);
+      }
+    }
+    for (int n = 0; n < S; ++n) {
+      const int slot = (int)(consumed % NST);
+      const bool ok = stage_wait(bar + slot, (consumed / NST) & 1u);
+      if (__any_sync(FULL, !ok)) {
+        if (lane == 0) atomicOr(a.err, 2);
+        abort = true;
+        break;
+      }
+      const StageGeo sg = geo[slot];
+      const float ds = sg.ds;
+      const float *rq = reinterpret_cast<const float *>(rows + (size_t)slot * rowbytes);
+      const MixedFit fit = (MODE == MODE_MIXED && QUAD) ? mixed_fit(a, sg.zin, mu, mu2) : MixedFit{};
+#pragma unroll
+      for (int k = 0; k < CPL; ++k) {
+        const int c = li + TPW * k;
+        if (c >= a.nchunk) continue;
+        const int g4 = 4 * c;
+        const float *cf = a.coef + sg.crow + 4 * COEF_PLANES * c;
+        const float4 sig = __ldg(reinterpret_cast<const float4 *>(cf));
+        const float4 r1 = __ldg(reinterpret_cast<const float4 *>(cf + 4));
+        float4 t;
+        const float4 y1 = *reinterpret_cast<const float4 *>(rq + g4);
+        if (QUAD) {
+          const float4 y2 = *reinterpret_cast<const float4 *>(rq + a.ldg + g4);
+          const float4 y3 = *reinterpret_cast<const float4 *>(rq + 2 * a.ldg + g4);
+          if (MODE == MODE_PLAIN) {
+            const float4 r2 = __ldg(reinterpret_cast<const float4 *>(cf + 8));
+            const float4 r3 = __ldg(reinterpret_cast<const float4 *>(cf + 12));
+            const float4 r4 = __ldg(reinterpret_cast<const float4 *>(cf + 16));
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+              const float sgm = get(sig, e);
+              const float sg2 = __fmul_rn(sgm, sgm);                      // solver.c:153
+              const float sg3 = __fmul_rn(sgm, sg2);                      // solver.c:176
+              const float sg4 = __fmul_rn(__fmul_rn(3.f, sg2), sg2);      // solver.c:198
+              float p = get(psi[k], e);
+              set(t, e, plain_quad(a, s_table, get(y1, e), get(y2, e), get(y3, e), sgm, sg2, sg3,
+                                   sg4, get(r1, e), get(r2, e), get(r3, e), get(r4, e), sg.zin,
+                                   ds, mu, mu2, w, p));
+              set(psi[k], e, p);
+            }
+          } else {
+            const float4 r2 = __ldg(reinterpret_cast<const float4 *>(cf + 8));
+            const float4 r4 = __ldg(reinterpret_cast<const float4 *>(cf + 16));
+            const float4 r3x2 = __ldg(reinterpret_cast<const float4 *>(cf + 20));
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+              float p = get(psi[k], e);
+              set(t, e, mixed_quad(get(y1, e), get(y2, e), get(y3, e), fit, get(sig, e),
+                                   get(r1, e), get(r2, e), get(r3x2, e), get(r4, e), ds, w, p));
+              set(psi[k], e, p);
+            }
+          }
+        } else {
+#pragma unroll
+          for (int e = 0; e < 4; ++e) {
+            float p = get(psi[k], e);
+            if (MODE == MODE_PLAIN)
+              set(t, e, plain_flat(a, s_table, get(y1, e), get(sig, e), get(r1, e), ds, w_mu, p));
+            else
+              set(t, e, mixed_flat(get(y1, e), get(sig, e), get(r1, e), ds, w_mu, p));
+            set(psi[k], e, p);
+          }
+        }
+        if (valid) {
+          float *dst = a.phi + sg.frow + g4;
+          if (MODE == MODE_MIXED && a.phi_lo != nullptr) {
+            float *lo = a.phi_lo + sg.frow + g4;
+            comp_add(dst + 0, lo + 0, t.x);
+            comp_add(dst + 1, lo + 1, t.y);
+            comp_add(dst + 2, lo + 2, t.z);
+            comp_add(dst + 3, lo + 3, t.w);
+          } else {
+            red_add_v4(dst, t.x, t.y, t.z, t.w);
+          }
+        }
+      }
+      ++consumed;
+      __syncwarp();                            // the stage is read: it may be refilled
+      if (pc.base < a.n3d) issue();
+    }
+    if (abort) break;
+    if (valid) {
+#pragma unroll
+      for (int k = 0; k < CPL; ++k) {
+        const int c = li + TPW * k;
+        if (c < a.nchunk) *reinterpret_cast<float4 *>(a.psi + tr * a.ldg + 4 * c) = psi[k];
+      }
+    }
+  }
+  // copies still in flight (only after an expired wait) land before the block exits
+  for (; consumed < issued; ++consumed)
+    stage_wait(bar + consumed % NST, (consumed / NST) & 1u);
+}
+
 // Chunks of 4 groups per thread in the batched kernel: with threads per track
 // from 4 to 32 this covers 8 to 256 groups.
 constexpr int BATCH_CPL = 2;
@@ -666,6 +941,48 @@ int dispatch_shape(moc_problem *p, const SweepArgs &a, int tpw, int cpl) {
   return MOC_ERR_UNSUPPORTED;
 }
 
+// Shared memory of the staged kernel: table, barriers, stage geometry, rows.
+size_t staged_smem(const SweepArgs &a, int mode, bool quad, int tpw, int nst) {
+  const size_t groups = BLOCK / tpw;
+  const size_t tab = mode == MODE_PLAIN ? (sizeof(float2) * a.table_n + 127) / 128 * 128 : 0;
+  const size_t rowbytes = (quad ? 3 : 1) * (size_t)a.ldg * 4;
+  return tab + (groups * nst * 8 + 127) / 128 * 128 +
+         (groups * nst * sizeof(StageGeo) + 127) / 128 * 128 + groups * nst * rowbytes;
+}
+
+template <int TPW, int CPL, int MODE, bool QUAD, int NST>
+int launch_staged_t(moc_problem *p, const SweepArgs &a) {
+  auto kern = sweep_staged_kernel<TPW, CPL, MODE, QUAD, NST>;
+  const size_t smem = staged_smem(a, MODE, QUAD, TPW, NST);
+  if (smem > 227 * 1024) return MOC_ERR_UNSUPPORTED;
+  MOC_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  int per_sm = 0, sms = 0;
+  MOC_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BLOCK, smem));
+  MOC_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p->device));
+  if (per_sm < 1) return MOC_ERR_UNSUPPORTED;
+  const int64_t warps = (a.n3d + (32 / TPW) - 1) / (32 / TPW);
+  const int64_t need = (warps + (BLOCK / 32) - 1) / (BLOCK / 32);
+  int64_t grid = (int64_t)per_sm * sms;
+  if (grid > need) grid = need;
+  if (grid < 1) grid = 1;
+  const int rowbytes = (QUAD ? 3 : 1) * a.ldg * 4;
+  kern<<<(unsigned)grid, BLOCK, smem, p->stream>>>(a, rowbytes);
+  MOC_CUDA_TRY(cudaGetLastError());
+  p->launches++;
+  return MOC_OK;
+}
+
+template <int MODE, bool QUAD>
+int dispatch_staged(moc_problem *p, const SweepArgs &a, int tpw, int cpl, int stages) {
+  if (stages != 4) return MOC_ERR_UNSUPPORTED;
+  if (tpw == 32 && cpl == 1) return launch_staged_t<32, 1, MODE, QUAD, 4>(p, a);
+  if (tpw == 32 && cpl == 2) return launch_staged_t<32, 2, MODE, QUAD, 4>(p, a);
+  if (tpw == 16 && cpl == 1) return launch_staged_t<16, 1, MODE, QUAD, 4>(p, a);
+  if (tpw == 16 && cpl == 2) return launch_staged_t<16, 2, MODE, QUAD, 4>(p, a);
+  if (tpw == 8 && cpl == 1) return launch_staged_t<8, 1, MODE, QUAD, 4>(p, a);
+  return MOC_ERR_UNSUPPORTED;
+}
+
 }  // namespace
 
 // Default threads-per-track and chunks-per-thread for a group count, from the
@@ -737,11 +1054,18 @@ SweepArgs build_args(moc_problem *p) {
   return a;
 }
 
-int launch_args(moc_problem *p, const SweepArgs &a, int tpw, int cpl) {
+int launch_args(moc_problem *p, const SweepArgs &a, int tpw, int cpl, int stages) {
   const bool quad = p->d.axial_exp == 2;
   if (p->mode == MOC_MODE_FP64) {
     if (!p->q64) return MOC_ERR_STATE;
     return quad ? launch64_t<32, true>(p, a) : launch64_t<32, false>(p, a);
+  }
+  if (stages > 0) {
+    if (p->mode == MOC_MODE_PLAIN)
+      return quad ? dispatch_staged<MODE_PLAIN, true>(p, a, tpw, cpl, stages)
+                  : dispatch_staged<MODE_PLAIN, false>(p, a, tpw, cpl, stages);
+    return quad ? dispatch_staged<MODE_MIXED, true>(p, a, tpw, cpl, stages)
+                : dispatch_staged<MODE_MIXED, false>(p, a, tpw, cpl, stages);
   }
   if (p->mode == MOC_MODE_PLAIN)
     return quad ? dispatch_shape<MODE_PLAIN, true>(p, a, tpw, cpl)
@@ -757,7 +1081,10 @@ struct TuneKey {
   }
 };
 std::mutex g_tune_mu;
-std::map<TuneKey, std::pair<int, int>> g_tune_cache;
+struct TuneChoice {
+  int tpw, cpl, stages;
+};
+std::map<TuneKey, TuneChoice> g_tune_cache;
 
 }  // namespace
 
@@ -765,7 +1092,7 @@ int moc_launch_sweep(moc_problem *p) {
   int tpw = 0, cpl = 0;
   int st = moc_sweep_launch_shape(p, &tpw, &cpl);
   if (st != MOC_OK) return st;
-  return launch_args(p, build_args(p), tpw, cpl);
+  return launch_args(p, build_args(p), tpw, cpl, p->stages > 0 ? p->stages : 0);
 }
 
 // A range of whole 2D tracks is a contiguous range of 3D tracks (the track
@@ -786,17 +1113,18 @@ int moc_launch_sweep_range(moc_problem *p, int64_t i2_begin, int64_t i2_end) {
   a.z0 += t0;
   a.psi += t0 * p->ldg;
   a.n3d = (i2_end - i2_begin) * P * Z;
-  return launch_args(p, a, tpw, cpl);
+  return launch_args(p, a, tpw, cpl, p->stages > 0 ? p->stages : 0);
 }
 
 // Times every launch shape that covers the groups on the first n_sub tracks.
 // Tallies go to a scratch copy of the flux array and the tracks' angular flux
 // to a scratch copy, so the problem's state is not changed.
 int moc_sweep_autotune(moc_problem *p, int64_t n_sub, int *tpw_out, int *cpl_out,
-                       double *ms_out) {
+                       int *stages_out, double *ms_out) {
   if (p->mode == MOC_MODE_FP64) {
     *tpw_out = 32;
     *cpl_out = 1;
+    *stages_out = 0;
     if (ms_out) *ms_out = 0.0;
     return MOC_OK;
   }
@@ -806,8 +1134,9 @@ int moc_sweep_autotune(moc_problem *p, int64_t n_sub, int *tpw_out, int *cpl_out
     std::lock_guard<std::mutex> lock(g_tune_mu);
     auto it = g_tune_cache.find(key);
     if (it != g_tune_cache.end() && ms_out == nullptr) {
-      *tpw_out = it->second.first;
-      *cpl_out = it->second.second;
+      *tpw_out = it->second.tpw;
+      *cpl_out = it->second.cpl;
+      *stages_out = it->second.stages;
       return MOC_OK;
     }
   }
@@ -835,19 +1164,25 @@ int moc_sweep_autotune(moc_problem *p, int64_t n_sub, int *tpw_out, int *cpl_out
       cudaMemcpyAsync(psi_s, p->psi_f, psi_bytes, cudaMemcpyDeviceToDevice, p->stream) !=
           cudaSuccess)
     rc = MOC_ERR_CUDA;
-  static const int shapes[][2] = {{32, 1}, {32, 2}, {32, 4}, {16, 1}, {16, 2}, {8, 1}, {8, 4}, {4, 2}};
+  // register-prefetch shapes, then the staged kernel (4-stage ring) shapes
+  static const int shapes[][3] = {{32, 1, 0}, {32, 2, 0}, {32, 4, 0}, {16, 1, 0}, {16, 2, 0},
+                                  {8, 1, 0},  {8, 4, 0},  {4, 2, 0},  {32, 1, 4}, {32, 2, 4},
+                                  {16, 1, 4}, {16, 2, 4}, {8, 1, 4}};
   const int nchunk = p->ldg / 4;
   double best = 1e30;
-  int bt = 0, bc = 0;
+  int bt = 0, bc = 0, bs = 0;
   for (auto &sh : shapes) {
     if (rc != MOC_OK) break;
     if ((int64_t)sh[0] * sh[1] < nchunk) continue;
     if ((int64_t)sh[0] * sh[1] >= 4 * (int64_t)nchunk && sh[1] > 1) continue;   // mostly idle lanes
-    rc = launch_args(p, a, sh[0], sh[1]);                    // warm-up
+    if (sh[2] > 0 && staged_smem(a, p->mode == MOC_MODE_PLAIN ? MODE_PLAIN : MODE_MIXED,
+                                 p->d.axial_exp == 2, sh[0], sh[2]) > 227 * 1024)
+      continue;
+    rc = launch_args(p, a, sh[0], sh[1], sh[2]);             // warm-up
     double tot = 0.0;
     for (int r = 0; r < 2 && rc == MOC_OK; ++r) {
       cudaEventRecord(p->ev0, p->stream);
-      rc = launch_args(p, a, sh[0], sh[1]);
+      rc = launch_args(p, a, sh[0], sh[1], sh[2]);
       cudaEventRecord(p->ev1, p->stream);
       if (rc == MOC_OK && cudaEventSynchronize(p->ev1) != cudaSuccess) rc = MOC_ERR_CUDA;
       float ms = 0.f;
@@ -858,6 +1193,7 @@ int moc_sweep_autotune(moc_problem *p, int64_t n_sub, int *tpw_out, int *cpl_out
       best = tot / 2;
       bt = sh[0];
       bc = sh[1];
+      bs = sh[2];
     }
   }
   cudaStreamSynchronize(p->stream);
@@ -868,10 +1204,11 @@ int moc_sweep_autotune(moc_problem *p, int64_t n_sub, int *tpw_out, int *cpl_out
   if (bt == 0) return MOC_ERR_UNSUPPORTED;
   {
     std::lock_guard<std::mutex> lock(g_tune_mu);
-    g_tune_cache[key] = {bt, bc};
+    g_tune_cache[key] = {bt, bc, bs};
   }
   *tpw_out = bt;
   *cpl_out = bc;
+  *stages_out = bs;
   if (ms_out) *ms_out = best;
   return MOC_OK;
 }

@@ -73,6 +73,16 @@ class Solver:
         L.check(self._lib.moc_set_launch(self._h, threads_per_track, chunks_per_thread),
                 "moc_set_launch")
 
+    def set_pipeline(self, stages: int) -> None:
+        """0: register prefetch of the next segment's rows; 4: a 4-stage
+        shared-memory ring filled by the bulk-copy engine; -1: automatic."""
+        L.check(self._lib.moc_set_pipeline(self._h, stages), "moc_set_pipeline")
+
+    def pipeline(self) -> int:
+        v = C.c_int()
+        L.check(self._lib.moc_get_pipeline(self._h, C.byref(v)), "moc_get_pipeline")
+        return int(v.value)
+
     def launch_shape(self) -> tuple[int, int]:
         a, b = C.c_int(), C.c_int()
         L.check(self._lib.moc_get_launch(self._h, C.byref(a), C.byref(b)), "moc_get_launch")

@@ -94,6 +94,60 @@ def test_plain_every_launch_shape_bit_exact(gpu_available, port, groups):
     assert ran >= 1
 
 
+STAGED_SHAPES = [(32, 1), (32, 2), (16, 1), (16, 2), (8, 1)]
+
+
+@pytest.mark.parametrize("groups,axial_exp", [(100, 2), (7, 2), (32, 0), (20, 2), (64, 0)])
+def test_staged_pipeline_bit_exact(gpu_available, port, groups, axial_exp):
+    """The 4-stage shared-memory ring (bulk copies): PLAIN psi equals the
+    oracle's bit for bit in every shape; MIXED psi equals the register
+    pipeline's (the same arithmetic on the same rows)."""
+    import simplemoc_gb300 as sm
+    spec = _spec(n_groups=groups, n_tracks_2d=16, z_stacked=10, axial_exp=axial_exp)
+    hp = sm.generate(spec)
+    st = oracle.fresh_state(hp)
+    op = oracle.make_problem(hp)
+    port.sweep(op, st["fine_source"], st["fine_flux"], st["psi_f"])
+    ldg = (groups + 3) // 4 * 4
+    ran = 0
+    for tpw, cpl in STAGED_SHAPES:
+        if tpw * cpl * 4 < ldg:
+            continue
+        with _solver(hp) as s:
+            s.set_launch(tpw, cpl)
+            s.set_pipeline(4)
+            s.transport_sweep()
+            out = s.download(psi_f=True, fine_flux=True)
+        assert np.array_equal(out["psi_f"], st["psi_f"]), (tpw, cpl)
+        assert rel_err(out["fine_flux"], st["fine_flux"]) <= PHI_TOL, (tpw, cpl)
+        psis = []
+        for stages in (0, 4):
+            with _solver(hp, mode="mixed") as s:
+                s.set_launch(tpw, cpl)
+                s.set_pipeline(stages)
+                s.transport_sweep()
+                psis.append(s.download(psi_f=True, fine_flux=False, fine_source=False)["psi_f"])
+        assert np.array_equal(psis[0], psis[1]), (tpw, cpl)
+        ran += 1
+    assert ran >= 1
+
+
+def test_staged_pipeline_power_iterations(gpu_available, port):
+    """Ten PLAIN power iterations through the staged sweep against the oracle,
+    several tracks per block and ragged track counts (13 x 3 x 7 tracks)."""
+    import simplemoc_gb300 as sm
+    spec = _spec(n_tracks_2d=13, n_polar=6, z_stacked=7, n_groups=40)
+    hp = sm.generate(spec)
+    st = oracle.fresh_state(hp)
+    ref_hist = port.iterate(hp, st, 10, threads=8)
+    with _solver(hp) as s:
+        s.set_pipeline(4)
+        hist = s.run(10)
+        out = s.download(psi_f=True, psi_b=True)
+    assert abs(hist[-1][0] - ref_hist[-1][0]) <= KEFF_TOL * abs(ref_hist[-1][0])
+    assert rel_err(out["psi_f"], st["psi_f"]) <= PHI_TOL
+
+
 @pytest.mark.parametrize("axial_exp", [2, 0])
 def test_plain_ten_power_iterations_vs_oracle(gpu_available, port, axial_exp):
     import simplemoc_gb300 as sm

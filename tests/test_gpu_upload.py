@@ -106,6 +106,14 @@ def test_upload_rejects_bad_source_ids(gpu_available):
     with sm.Solver(hp, mode="plain") as b:
         with pytest.raises(sm.MocError):
             b.upload(bad)
-        # the rejected upload changed nothing: the handle still sweeps
+        # the rejected upload overwrote part of the state: work is refused ...
+        with pytest.raises(sm.MocError):
+            b.transport_sweep()
+        # ... until a valid upload, after which the handle sweeps as a fresh one
+        b.upload(hp)
         b.transport_sweep()
-        b.synchronize()
+        out = b.download(psi_f=True, fine_flux=False, fine_source=False)
+    with sm.Solver(hp, mode="plain") as a:
+        a.transport_sweep()
+        ref = a.download(psi_f=True, fine_flux=False, fine_source=False)
+    assert np.array_equal(out["psi_f"], ref["psi_f"])
