@@ -166,58 +166,62 @@ struct TcArgs {
   uint32_t tmem_cols;          // 4 * acc_stride
 };
 
-// One thread's region row of a tile: material, the region (global row) and
-// whether the row exists (the last tile of a material is ragged).
-struct TileRow {
-  int m;
-  bool valid;
-  int64_t grow;
-};
+// Shared memory of the kernel (floats unless noted):
+//   region 0: A hi and lo, [kgroups][TC_A_LBO bytes] each (K groups padded by
+//             16 bytes: the coalesced staging stores are conflict-free); after
+//             the products the same space holds the accumulator rows
+//             D[128][np + 4] (a row stride of an odd number of 16-byte units)
+//   region 1: B hi and lo of the current material, then chi[G]
+//   region 2: the global row of each tile row, two buffers of 128 int64
+constexpr int TC_A_LBO = TC_M * 16 + 16;      // bytes between K groups of A
 
-__device__ __forceinline__ TileRow tile_row(const TcArgs &x, int it, int row) {
-  TileRow t{0, false, 0};
-  if (it >= x.n_items) return t;
-  t.m = x.items[3 * it];
+__host__ __device__ constexpr int tc_region0_bytes(int kp, int np) {
+  return (2 * (kp / 4) * TC_A_LBO > TC_M * (np + 4) * 4 ? 2 * (kp / 4) * TC_A_LBO
+                                                         : TC_M * (np + 4) * 4);
+}
+__host__ __device__ constexpr int tc_smem_bytes(int kp, int np, int G) {
+  return tc_region0_bytes(kp, np) + (2 * np * kp + (G + 3) / 4 * 4) * 4 + 2 * TC_M * 8;
+}
+
+// The global row (fine region) of tile row `row`, -1 beyond the tile.
+__device__ __forceinline__ int64_t tile_grow(const TcArgs &x, int it, int row) {
+  if (it >= x.n_items) return -1;
   const int s0 = x.items[3 * it + 1], s1 = x.items[3 * it + 2];
-  t.valid = row < (s1 - s0) * x.F;
-  if (t.valid) t.grow = (int64_t)x.xs_order[s0 + row / x.F] * x.F + row % x.F;
-  return t;
+  if (row >= (s1 - s0) * x.F) return -1;
+  return (int64_t)x.xs_order[s0 + row / x.F] * x.F + row % x.F;
 }
 
-// K groups j0 .. j1-1 of the row's fluxes, zero beyond G.
-__device__ __forceinline__ void load_fluxes(const TcArgs &x, const TileRow &t, int j0, int j1,
-                                            float4 (&buf)[(TC_MAX_KG + 1) / 2]) {
-  const float *prow = x.phi + t.grow * x.ldg;
-#pragma unroll
-  for (int i = 0; i < (TC_MAX_KG + 1) / 2; ++i) {
-    const int k = 4 * (j0 + i);
-    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (t.valid && j0 + i < j1 && k < x.ldg) v = ld_nc4(prow + k);
-    if (k + 0 >= x.G) v.x = 0.f;
-    if (k + 1 >= x.G) v.y = 0.f;
-    if (k + 2 >= x.G) v.z = 0.f;
-    if (k + 3 >= x.G) v.w = 0.f;
-    buf[i] = v;
-  }
-}
+// Each warp moves 16 rows of a tile as (row, K group) pairs, lane-consecutive
+// along the row: element e = lane + 32 t of warp w is row 16 w + e / kgroups,
+// K group e % kgroups.  rk[t] packs (row << 8) | kgroup, -1 past the warp's rows.
+constexpr int TC_PER_LANE = (16 * TC_MAX_KG + 31) / 32;   // 13
 
 __global__ void __launch_bounds__(TC_THREADS, 1) update_tc_kernel(TcArgs x) {
-  extern __shared__ __align__(128) float tc_smem[];
+  extern __shared__ __align__(128) unsigned char tc_smem[];
   __shared__ __align__(8) uint64_t bar;
   __shared__ uint32_t tmem_base;
   __shared__ int abort_flag;
   __shared__ double sh[TC_THREADS / 32];
-  const int tid = threadIdx.x, warp = tid >> 5;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int row = tid & (TC_M - 1);            // = (warp % 4) * 32 + lane: its TMEM lane
-  const int half = tid >> 7;                   // 0: first half of the K groups / columns
+  const int half = tid >> 7;                   // 0: first half of the accumulator columns
   const int KP = x.kp, NP = x.np, G = x.G, ldg = x.ldg;
-  float *a_hi = tc_smem;
-  float *a_lo = a_hi + TC_M * KP;
-  float *b_hi = a_lo + TC_M * KP;              // b_lo follows b_hi: one copy per material
-  float *b_lo = b_hi + NP * KP;
   const int kgroups = KP / 4;
-  const int jh = (kgroups + 1) / 2;
-  const int j0 = half ? jh : 0, j1 = half ? kgroups : jh;
+  const int DS = NP + 4;                       // accumulator row stride in shared memory
+  unsigned char *a_hi = tc_smem;
+  unsigned char *a_lo = a_hi + kgroups * TC_A_LBO;
+  float *d_s = reinterpret_cast<float *>(tc_smem);                  // after the products
+  float *b_hi = reinterpret_cast<float *>(tc_smem + tc_region0_bytes(KP, NP));
+  float *b_lo = b_hi + NP * KP;
+  float *chi_s = b_lo + NP * KP;
+  int64_t *grow_s = reinterpret_cast<int64_t *>(chi_s + (G + 3) / 4 * 4);   // [2][128]
+
+  int rk[TC_PER_LANE];
+#pragma unroll
+  for (int t = 0; t < TC_PER_LANE; ++t) {
+    const int e = lane + 32 * t;
+    rk[t] = e < 16 * kgroups ? ((16 * warp + e / kgroups) << 8) | (e % kgroups) : -1;
+  }
 
   if (warp == 0) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
@@ -232,6 +236,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1) update_tc_kernel(TcArgs x) {
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     abort_flag = 0;
   }
+  int it = blockIdx.x;
+  int cur_buf = 0;
+  if (tid < TC_M) grow_s[tid] = tile_grow(x, it, tid);
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
@@ -249,35 +256,51 @@ __global__ void __launch_bounds__(TC_THREADS, 1) update_tc_kernel(TcArgs x) {
   double res_acc = 0.0, abs_acc = 0.0, fis_acc = 0.0;
   uint32_t phase = 0;
   int cur_m = -1;
-
-  // Software pipeline over this block's tiles: while the tensor core works on
-  // tile i, the registers receive tile i+1's fluxes and tile i's old sources.
-  constexpr int HKG = (TC_MAX_KG + 1) / 2;      // K groups per thread
-  const int nch = (G + 15) / 16;                // 16-column chunks holding groups
+  const int nch = (NP + 15) / 16;               // 16-column chunks of the product
   const int ch_split = (nch + 1) / 2;
   const int c0 = half ? ch_split : 0, c1 = half ? nch : ch_split;
-  float4 buf[HKG];
-  int it = blockIdx.x;
-  TileRow cur = tile_row(x, it, row);
-  load_fluxes(x, cur, j0, j1, buf);
+
+  // this tile's fluxes, coalesced: row-consecutive 16-byte pieces per lane
+  float4 buf[TC_PER_LANE];
+  auto load_fluxes = [&](const int64_t *gs) {
+#pragma unroll
+    for (int t = 0; t < TC_PER_LANE; ++t) {
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (rk[t] >= 0) {
+        const int64_t gr = gs[rk[t] >> 8];
+        const int k = 4 * (rk[t] & 255);
+        if (gr >= 0 && k < ldg) v = ld_nc4(x.phi + gr * ldg + k);
+        if (k + 0 >= G) v.x = 0.f;
+        if (k + 1 >= G) v.y = 0.f;
+        if (k + 2 >= G) v.z = 0.f;
+        if (k + 3 >= G) v.w = 0.f;
+      }
+      buf[t] = v;
+    }
+  };
+  load_fluxes(grow_s);
+
   while (it < x.n_items) {
-    if (cur.m != cur_m) {                       // the same on every thread
-      const uint4 *src = reinterpret_cast<const uint4 *>(x.bmat + (int64_t)cur.m * 2 * NP * KP);
+    const int m = x.items[3 * it];
+    const int64_t *gcur = grow_s + cur_buf * TC_M;
+    int64_t *gnext = grow_s + (cur_buf ^ 1) * TC_M;
+    if (m != cur_m) {                          // the same on every thread
+      const uint4 *src = reinterpret_cast<const uint4 *>(x.bmat + (int64_t)m * 2 * NP * KP);
       uint4 *dst = reinterpret_cast<uint4 *>(b_hi);
       for (int i = tid; i < 2 * NP * KP / 4; i += TC_THREADS) dst[i] = __ldg(src + i);
-      cur_m = cur.m;
+      for (int i = tid; i < G; i += TC_THREADS) chi_s[i] = __ldg(x.xs + ((int64_t)m * G + i) * 3 + 2);
+      cur_m = m;
     }
-    // ---- A: this row's fluxes split into TF32 hi and lo (lo rounded as well:
-    // the tensor core would otherwise drop its low 13 bits, a bias to zero)
+    // ---- A: the fluxes split into TF32 hi and lo (lo rounded as well: the
+    // tensor core would otherwise drop its low 13 bits, a bias to zero)
 #pragma unroll
-    for (int t = 0; t < HKG; ++t) {
-      const int j = j0 + t;
-      if (j >= j1) continue;
+    for (int t = 0; t < TC_PER_LANE; ++t) {
+      if (rk[t] < 0) continue;
       const float4 v = buf[t];
       const float4 hi = make_float4(to_tf32(v.x), to_tf32(v.y), to_tf32(v.z), to_tf32(v.w));
       const float4 lo = make_float4(to_tf32(v.x - hi.x), to_tf32(v.y - hi.y),
                                     to_tf32(v.z - hi.z), to_tf32(v.w - hi.w));
-      const int off = j * (TC_M * 4) + row * 4;
+      const int off = (rk[t] & 255) * TC_A_LBO + (rk[t] >> 8) * 16;
       *reinterpret_cast<float4 *>(a_hi + off) = hi;
       *reinterpret_cast<float4 *>(a_lo + off) = lo;
     }
@@ -286,12 +309,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1) update_tc_kernel(TcArgs x) {
     // ---- the products, K steps of 8, issued by one thread
     if (tid == 0) {
       tc_fence_after();
-      const uint32_t lbo_a = TC_M * 16, lbo_b = (uint32_t)NP * 16;
+      const uint32_t lbo_b = (uint32_t)NP * 16;
       const uint32_t ah = smem_u32(a_hi), al = smem_u32(a_lo);
       const uint32_t bh = smem_u32(b_hi), bl = smem_u32(b_lo);
       for (int kk = 0; kk < ksteps; ++kk) {
-        const uint64_t dah = mma_desc(ah + kk * 2 * lbo_a, lbo_a, 128);
-        const uint64_t dal = mma_desc(al + kk * 2 * lbo_a, lbo_a, 128);
+        const uint64_t dah = mma_desc(ah + kk * 2 * TC_A_LBO, TC_A_LBO, 128);
+        const uint64_t dal = mma_desc(al + kk * 2 * TC_A_LBO, TC_A_LBO, 128);
         const uint64_t dbh = mma_desc(bh + kk * 2 * lbo_b, lbo_b, 128);
         const uint64_t dbl = mma_desc(bl + kk * 2 * lbo_b, lbo_b, 128);
         const int chain = kk * n_chain / ksteps;
@@ -302,17 +325,19 @@ __global__ void __launch_bounds__(TC_THREADS, 1) update_tc_kernel(TcArgs x) {
       }
       mma_commit(&bar);
     }
-    // ---- meanwhile: the next tile's fluxes and this tile's old sources
+    // ---- meanwhile: the next tile's rows and fluxes, this tile's old sources
     const int nx = it + (int)gridDim.x;
-    const TileRow nxt = tile_row(x, nx, row);
-    load_fluxes(x, nxt, j0, j1, buf);
-    float4 qold[16];
+    if (tid < TC_M) gnext[tid] = tile_grow(x, nx, tid);
+    __syncthreads();
+    load_fluxes(gnext);
+    float4 qold[TC_PER_LANE];
 #pragma unroll
-    for (int t = 0; t < 16; ++t) {
-      const int g = 16 * c0 + 4 * t;
+    for (int t = 0; t < TC_PER_LANE; ++t) {
       qold[t] = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (cur.valid && g < 16 * c1 && g < ldg)
-        qold[t] = *reinterpret_cast<const float4 *>(x.q + cur.grow * ldg + g);
+      if (rk[t] < 0) continue;
+      const int64_t gr = gcur[rk[t] >> 8];
+      const int k = 4 * (rk[t] & 255);
+      if (gr >= 0 && k < ldg) qold[t] = *reinterpret_cast<const float4 *>(x.q + gr * ldg + k);
     }
     if (tid == 0) {
       if (!wait_phase(&bar, phase)) {
@@ -325,64 +350,58 @@ __global__ void __launch_bounds__(TC_THREADS, 1) update_tc_kernel(TcArgs x) {
     if (abort_flag) break;
     phase ^= 1u;
     tc_fence_after();
-    // ---- epilogue: fission and absorption columns G and G + 1, then the groups
-    float fis = 0.f, absr = 0.f;
-    {
-      float v[16];
-      acc_ld16(taddr + (uint32_t)(G & ~15), AS, n_chain, v);
+    // ---- the accumulator rows to shared memory (A is consumed), one thread
+    // per row and half of its 16-column chunks
 #pragma unroll
-      for (int e = 0; e < 16; ++e) {
-        if (e == (G & 15)) fis = v[e];
-        if (e == ((G + 1) & 15) && ((G + 1) & ~15) == (G & ~15)) absr = v[e];
-      }
-      if (((G + 1) & ~15) != (G & ~15)) {
-        acc_ld16(taddr + (uint32_t)((G + 1) & ~15), AS, n_chain, v);
-        absr = v[0];
-      }
-    }
-    const float fk = __fmul_rn(fis, inverse_k);
-    float res_row = 0.f;
-#pragma unroll
-    for (int cc = 0; cc < 4; ++cc) {            // this thread's chunks c0 .. c1-1
+    for (int cc = 0; cc < 4; ++cc) {
       const int c = c0 + cc;
-      if (c >= c1) break;                       // the same on every lane of a warp
+      if (c >= c1) break;                      // the same on every lane of a warp
       float v[16];
       acc_ld16(taddr + (uint32_t)(16 * c), AS, n_chain, v);
-#pragma unroll
-      for (int qv = 0; qv < 4; ++qv) {
-        const int g = 16 * c + 4 * qv;
-        if (!cur.valid || g >= ldg) continue;
-        const float4 old = qold[4 * cc + qv];
-        float4 nw = old;
-        const float *po = &old.x;
-        float *pn = &nw.x;
-#pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          const int gg = g + e;
-          if (gg >= G) continue;
-          const float chi = __ldg(x.xs + ((int64_t)cur.m * G + gg) * 3 + 2);
-          // src/solver.c:1289-1295
-          const float num = __fadd_rn(__fmul_rn(fk, chi), v[4 * qv + e]);
-          float qq = __fmul_rn(num, r_four_pi);
-          qq = __fmaf_rn(__fmaf_rn(-qq, four_pi, num), r_four_pi, qq);
-          pn[e] = qq;
-          const float d = qq - po[e];
-          res_row += __fdividef(d * d, po[e] * po[e]);   // a diagnostic: fast quotient
-        }
-        *reinterpret_cast<float4 *>(x.q + cur.grow * ldg + g) = nw;
-      }
-    }
-    if (cur.valid) {
-      res_acc += (double)res_row;
-      if (half == 0) {
-        abs_acc += (double)absr;
-        fis_acc += (double)fis;
-      }
+      float4 *dr = reinterpret_cast<float4 *>(d_s + row * DS + 16 * c);
+      dr[0] = make_float4(v[0], v[1], v[2], v[3]);
+      dr[1] = make_float4(v[4], v[5], v[6], v[7]);
+      dr[2] = make_float4(v[8], v[9], v[10], v[11]);
+      dr[3] = make_float4(v[12], v[13], v[14], v[15]);
     }
     tc_fence_before();
-    __syncthreads();                            // TMEM read and A consumed: next tile
+    __syncthreads();
+    if (tid < TC_M && gcur[tid] >= 0) {        // the k_eff sums: columns G and G + 1
+      fis_acc += (double)d_s[tid * DS + G];
+      abs_acc += (double)d_s[tid * DS + G + 1];
+    }
+    // ---- the new sources, coalesced along the rows
+    float res = 0.f;
+#pragma unroll
+    for (int t = 0; t < TC_PER_LANE; ++t) {
+      if (rk[t] < 0) continue;
+      const int r = rk[t] >> 8, g = 4 * (rk[t] & 255);
+      const int64_t gr = gcur[r];
+      if (gr < 0 || g >= ldg) continue;
+      const float4 d4 = *reinterpret_cast<const float4 *>(d_s + r * DS + g);
+      const float fk = __fmul_rn(d_s[r * DS + G], inverse_k);
+      const float *pd = &d4.x;
+      const float4 old = qold[t];
+      float4 nw = old;
+      const float *po = &old.x;
+      float *pn = &nw.x;
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        if (g + e >= G) continue;
+        // src/solver.c:1289-1295
+        const float num = __fadd_rn(__fmul_rn(fk, chi_s[g + e]), pd[e]);
+        float qq = __fmul_rn(num, r_four_pi);
+        qq = __fmaf_rn(__fmaf_rn(-qq, four_pi, num), r_four_pi, qq);
+        pn[e] = qq;
+        const float dd = qq - po[e];
+        res += __fdividef(dd * dd, po[e] * po[e]);   // a diagnostic: fast quotient
+      }
+      *reinterpret_cast<float4 *>(x.q + gr * ldg + g) = nw;
+    }
+    res_acc += (double)res;
+    __syncthreads();                           // the shared rows are read: next tile
     it = nx;
-    cur = nxt;
+    cur_buf ^= 1;
   }
   // ---- teardown: with the products drained, free the tensor memory
   if (abort_flag && tid == 0) wait_phase(&bar, phase);
@@ -410,12 +429,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1) update_tc_kernel(TcArgs x) {
 int moc_launch_update_tc(moc_problem *p) {
   const int kp = p->tc_kp, np = p->tc_np;
   if (!p->tc_b || kp == 0 || p->n_tc_items < 1) return MOC_ERR_UNSUPPORTED;
-  const size_t smem = sizeof(float) * (2 * (size_t)TC_M * kp + 2 * (size_t)np * kp);
+  const size_t smem = (size_t)tc_smem_bytes(kp, np, p->d.n_groups);
   // set outside any stream capture by the first call (the largest operands)
   static bool attr_set = false;
   if (!attr_set) {
-    const size_t max_smem =
-        sizeof(float) * (2 * (size_t)TC_M * 4 * TC_MAX_KG + 2 * (size_t)MOC_TC_MAX_NP * 4 * TC_MAX_KG);
+    const size_t max_smem = (size_t)tc_smem_bytes(4 * TC_MAX_KG, MOC_TC_MAX_NP, 4 * TC_MAX_KG);
     MOC_CUDA_TRY(cudaFuncSetAttribute(update_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)max_smem));
     attr_set = true;
