@@ -115,7 +115,7 @@ int upload_all(moc_problem *p, const moc_host *h, bool stream_tracks) {
     MOC_CUDA_TRY(cudaStreamWaitEvent(p->copy_stream, p->main_ev, 0));
     TRY(put_rows(p, p->q, h->fine_source, p->nfsr));
     TRY(put_rows(p, p->phi, h->fine_flux, p->nfsr));
-    TRY(moc_host_validate(&d, h));
+    TRY(moc_host_validate_except_ids(&d, h));   // the ids chunk by chunk, below
   }
   std::vector<float> seg_ds((size_t)(N2D * P * S)), mu((size_t)P), weight((size_t)p->n3d);
   std::vector<float> coef((size_t)d.n_sigt * COEF_PLANES * p->ldg);
@@ -220,6 +220,8 @@ int upload_all(moc_problem *p, const moc_host *h, bool stream_tracks) {
     for (int k = 0; k < n; ++k) {
       const int64_t i0 = N2D * k / n, i1 = N2D * (k + 1) / n;
       const int64_t t0 = i0 * PZ, nt = (i1 - i0) * PZ;
+      // this chunk's source ids are checked while the previous chunk copies
+      TRY(moc_host_validate_ids(&d, h, t0 * S, (t0 + nt) * S));
       TRY(put(p, p->seg_src + t0 * S, h->seg_src + t0 * S, nt * S, p->copy_stream));
       TRY(put_rows(p, p->psi_f + t0 * p->ldg, h->psi_f ? h->psi_f + t0 * G : nullptr, nt,
                    p->copy_stream));

@@ -238,7 +238,23 @@ void moc_host_coef(const moc_dims *d, const float *sigt, int32_t ldg, float *coe
   }
 }
 
+int moc_host_validate_ids(const moc_dims *d, const moc_host *h, int64_t first, int64_t end) {
+  const int64_t NS = d->n_sources;
+  const int32_t *ids = h->seg_src;
+  int bad = 0;
+#pragma omp parallel for schedule(static) reduction(| : bad)
+  for (int64_t k = first; k < end; k++) bad |= (ids[k] < 0 || ids[k] >= NS);
+  return bad ? MOC_ERR_ARG : MOC_OK;
+}
+
 int moc_host_validate(const moc_dims *d, const moc_host *h) {
+  int rc = moc_host_validate_except_ids(d, h);
+  if (rc != MOC_OK) return rc;
+  return moc_host_validate_ids(d, h, 0,
+                               d->n_tracks_2d * d->n_polar * d->z_stacked * (int64_t)d->n_seg);
+}
+
+int moc_host_validate_except_ids(const moc_dims *d, const moc_host *h) {
   const int64_t G = d->n_groups, NS = d->n_sources, N3D = d->n_tracks_2d * d->n_polar * d->z_stacked;
   const int64_t S = d->n_seg;
   if (G < 1 || d->fai < 1 || d->cai < 1 || d->decomp_ax < 1 || NS < 1 || d->n_sigt < 1 ||
@@ -265,9 +281,6 @@ int moc_host_validate(const moc_dims *d, const moc_host *h) {
   for (int64_t k = 0; k < (int64_t)d->n_sigt * G; k++)
     if (!(h->sigt[k] > 0.0f) || isinf(h->sigt[k])) return MOC_ERR_ARG;
   int bad = 0;
-#pragma omp parallel for schedule(static) reduction(| : bad)
-  for (int64_t k = 0; k < N3D * S; k++) bad |= (h->seg_src[k] < 0 || h->seg_src[k] >= NS);
-  if (bad) return MOC_ERR_ARG;
 #pragma omp parallel for schedule(static) reduction(| : bad)
   for (int64_t k = 0; k < d->n_tracks_2d * S; k++)
     bad |= !(h->seg_len[k] >= 0.0f) || isinf(h->seg_len[k]);
