@@ -44,7 +44,8 @@ def _args():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--config", choices=["default", "small", "default_1k", "batched", "adjoint"],
+    ap.add_argument("--config", choices=["default", "small", "default_1k", "batched", "adjoint",
+                                         "dropin"],
                     default="default")
     ap.add_argument("--cores", type=int, default=64, help="cores of the batched workload")
     ap.add_argument("--no-e2e", action="store_true")
@@ -343,9 +344,74 @@ def run_adjoint(args):
     print(json.dumps(line), flush=True)
 
 
+def run_dropin(args):
+    """The drop-in: the reference's own entry points (transport_sweep,
+    renormalize_flux, update_sources, compute_keff with the reference's structs,
+    include/simplemoc_refabi.h) on a reference-layout problem of the small
+    problem's size: 1024 2D tracks of ~50 segments, 4 polar angles, 300 stacked
+    rays over 200 cm, 100 groups.  The traversal is the reference's (axial
+    splitting, stacked-ray retirement) in PLAIN arithmetic; source ids come from
+    the counter hash (the libc rand() sequence is drawn on the host, for parity
+    runs).  A step is one power iteration through the four symbols (each returns
+    on the host, as the reference's do); integrations = the traversal's 3D
+    sub-segments x groups."""
+    import ctypes as C
+
+    import simplemoc_gb300 as sm
+    from simplemoc_gb300 import refabi
+    spec = sm.CONFIG_SMALL
+    hp = sm.generate(spec, with_state=False)
+    Z = spec.z_stacked
+    geo = refabi.make_geometry(spec.seed + 1, spec.n_tracks_2d, spec.n_polar, Z, 50.0,
+                               spec.height / Z)
+    rp = refabi.build(hp, geo)
+    lb = refabi.lib()
+    lb.moc_ref_finalize()
+    lb.moc_ref_set_rng(refabi.RNG_HASH, 1234)
+    grid = refabi.CommGrid()
+    keff = [1.0]
+
+    def step():
+        lb.transport_sweep(C.byref(rp.params), C.byref(rp.input))
+        lb.renormalize_flux(rp.params, rp.input, grid)
+        lb.update_sources(rp.params, rp.input, keff[0])
+        keff[0] = lb.compute_keff(rp.params, rp.input, grid)
+        if lb.moc_ref_status() != 0:
+            raise RuntimeError(f"drop-in status {lb.moc_ref_status()}")
+        return int(lb.moc_ref_last_segments())
+
+    K, W = max(1, args.steps), max(1, args.warmup)
+    for _ in range(W):
+        step()
+    t0 = time.perf_counter()
+    segs = sum(step() for _ in range(K))
+    dt = time.perf_counter() - t0
+    lb.moc_ref_finalize()
+    G = spec.n_groups
+    line = {
+        "metric": "segment-group integrations/s per power iteration through the reference's "
+                  "entry points", "value": segs * G / dt, "unit": "integrations/s",
+        "n_gpus": 1, "steps": K, "warmup": W, "ms_per_step": 1e3 * dt / K,
+        "higher_is_better": True, "dtype": "f32", "data": "synthetic (seeded)",
+        "config": {"workload": f"drop-in: {spec.n_tracks_2d} 2D tracks x {spec.n_polar} polar x "
+                               f"{Z} stacked rays, {G} groups, reference traversal, PLAIN",
+                   "sub_segments_per_sweep": segs // K},
+        "keff": keff[0],
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = _args()
     import simplemoc_gb300 as sm
+    if args.config == "dropin":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable":
+                              "the drop-in line times this library through the reference's "
+                              "symbols; the reference arm is the default config's"}))
+            return
+        run_dropin(args)
+        return
     if args.config == "adjoint":
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable":

@@ -152,10 +152,24 @@ class RefProblem:
         return np.array([t.z_height for t in self.tracks], dtype=np.float32)
 
 
+def _struct_array(ctype, n: int) -> tuple[np.ndarray, object]:
+    """A zeroed numpy record array with the field offsets and size of the
+    ctypes structure `ctype`, and the ctypes array view of the same memory."""
+    names = [f[0] for f in ctype._fields_]
+    fmt = {C.c_float: "<f4", C.c_long: "<i8", C.c_int: "<i4", C.c_bool: "u1"}
+    formats = [fmt.get(f[1], "<u8") for f in ctype._fields_]     # pointers: 8-byte addresses
+    offsets = [getattr(ctype, nm).offset for nm in names]
+    dt = np.dtype({"names": names, "formats": formats, "offsets": offsets,
+                   "itemsize": C.sizeof(ctype)})
+    arr = np.zeros(max(1, n), dtype=dt)
+    return arr, (ctype * max(1, n)).from_buffer(arr)
+
+
 def build(hp, geo: RefGeometry, precision: float | None = None) -> RefProblem:
     """Reference-layout problem: sources / cross sections of the HostProblem
     `hp` (one sigma_t row per source, as src/source.c:150-152), 2D tracks and
-    stacked rays of `geo`."""
+    stacked rays of `geo`.  The structs are filled through numpy views of
+    their memory (millions of tracks at the default sizes)."""
     s = hp.spec
     G, F, NS, P = s.n_groups, s.fai, s.n_sources, s.n_polar
     N2D = len(geo.seg_off) - 1
@@ -166,58 +180,44 @@ def build(hp, geo: RefGeometry, precision: float | None = None) -> RefProblem:
     psi_f = np.zeros(N2D * P * Z * G, np.float32)
     psi_b = np.zeros_like(psi_f)
     sigt_rows = np.ascontiguousarray(hp.sigt.reshape(-1, G)[hp.src_sigt])   # [NS][G]
-    xs3 = hp.xs.reshape(-1, G, 3)
-    sc = hp.scatter.reshape(-1, G, G)
+    xs3 = np.ascontiguousarray(hp.xs.reshape(-1, G, 3))
+    sc = np.ascontiguousarray(hp.scatter.reshape(-1, G, G))
     n_xs = xs3.shape[0]
-    xs_rows = (fp * (n_xs * G))()
-    sc_rows = (fp * (n_xs * G))()
-    for m in range(n_xs):
-        for g in range(G):
-            xs_rows[m * G + g] = xs3[m, g].ctypes.data_as(fp)
-            sc_rows[m * G + g] = sc[m, g].ctypes.data_as(fp)
-    q_rows = (fp * (NS * F))()
-    f_rows = (fp * (NS * F))()
-    base_q, base_f = q.ctypes.data, phi.ctypes.data
-    for r in range(NS * F):
-        q_rows[r] = C.cast(base_q + 4 * r * G, fp)
-        f_rows[r] = C.cast(base_f + 4 * r * G, fp)
-    sources = (Source * NS)()
-    for i in range(NS):
-        src = sources[i]
-        src.fine_source = C.cast(C.addressof(q_rows) + 8 * i * F, fpp)
-        src.fine_flux = C.cast(C.addressof(f_rows) + 8 * i * F, fpp)
-        src.vol = float(hp.vol[i])
-        src.sigT = C.cast(sigt_rows.ctypes.data + 4 * i * G, fp)
-        m = int(hp.src_xs[i])
-        src.XS = C.cast(C.addressof(xs_rows) + 8 * m * G, fpp)
-        src.scattering_matrix = C.cast(C.addressof(sc_rows) + 8 * m * G, fpp)
-    segs = (Segment * max(1, int(geo.seg_off[-1])))()
-    for k, ln in enumerate(geo.seg_len):
-        segs[k].length = float(ln)
-    t2d = (Track2D * N2D)()
-    for i in range(N2D):
-        t2d[i].az_weight = float(geo.az_weight[i])
-        t2d[i].n_segments = int(geo.seg_off[i + 1] - geo.seg_off[i])
-        t2d[i].segments = C.cast(C.addressof(segs) + C.sizeof(Segment) * int(geo.seg_off[i]),
-                                 C.POINTER(Segment))
+    # row pointer tables: XS[m][g] -> 3 floats, scatter[m][g] -> G floats
+    xs_rows = xs3.ctypes.data + 12 * np.arange(n_xs * G, dtype=np.uint64)
+    sc_rows = sc.ctypes.data + 4 * G * np.arange(n_xs * G, dtype=np.uint64)
+    q_rows = q.ctypes.data + 4 * G * np.arange(NS * F, dtype=np.uint64)
+    f_rows = phi.ctypes.data + 4 * G * np.arange(NS * F, dtype=np.uint64)
+    src_arr, sources = _struct_array(Source, NS)
+    i = np.arange(NS, dtype=np.uint64)
+    m = hp.src_xs.astype(np.uint64)
+    src_arr["fine_source"] = q_rows.ctypes.data + 8 * F * i
+    src_arr["fine_flux"] = f_rows.ctypes.data + 8 * F * i
+    src_arr["vol"] = hp.vol
+    src_arr["sigT"] = sigt_rows.ctypes.data + 4 * G * i
+    src_arr["XS"] = xs_rows.ctypes.data + 8 * G * m
+    src_arr["scattering_matrix"] = sc_rows.ctypes.data + 8 * G * m
+    seg_arr, segs = _struct_array(Segment, int(geo.seg_off[-1]))
+    seg_arr["length"][:len(geo.seg_len)] = geo.seg_len
+    t2d_arr, t2d = _struct_array(Track2D, N2D)
+    t2d_arr["az_weight"] = geo.az_weight
+    t2d_arr["n_segments"] = np.diff(geo.seg_off)
+    t2d_arr["segments"] = C.addressof(segs) + C.sizeof(Segment) * geo.seg_off[:-1].astype(np.uint64)
     n3d = N2D * P * Z
-    tracks = (Track * n3d)()
-    for t in range(n3d):
-        tracks[t].p_weight = float(geo.p_weight[t])
-        tracks[t].z_height = float(geo.z_height[t])
-        tracks[t].f_psi = C.cast(psi_f.ctypes.data + 4 * t * G, fp)
-        tracks[t].b_psi = C.cast(psi_b.ctypes.data + 4 * t * G, fp)
-    rows = (C.POINTER(Track) * (N2D * P))()
-    for r in range(N2D * P):
-        rows[r] = C.cast(C.addressof(tracks) + C.sizeof(Track) * r * Z, C.POINTER(Track))
-    tr3 = (C.POINTER(C.POINTER(Track)) * N2D)()
-    for i in range(N2D):
-        tr3[i] = C.cast(C.addressof(rows) + 8 * i * P, C.POINTER(C.POINTER(Track)))
+    trk_arr, tracks = _struct_array(Track, n3d)
+    t = np.arange(n3d, dtype=np.uint64)
+    trk_arr["p_weight"] = geo.p_weight
+    trk_arr["z_height"] = geo.z_height
+    trk_arr["f_psi"] = psi_f.ctypes.data + 4 * G * t
+    trk_arr["b_psi"] = psi_b.ctypes.data + 4 * G * t
+    rows = C.addressof(tracks) + C.sizeof(Track) * Z * np.arange(N2D * P, dtype=np.uint64)
+    tr3 = rows.ctypes.data + 8 * P * np.arange(N2D, dtype=np.uint64)
+    keep += [src_arr, seg_arr, t2d_arr, trk_arr]
     leak = (C.c_float * 1)(0.0)
     polar = np.ascontiguousarray(hp.polar_angles, dtype=np.float32)
     table = np.ascontiguousarray(hp.table, dtype=np.float32)
     prm = Params(tracks_2D=C.cast(t2d, C.POINTER(Track2D)),
-                 tracks=C.cast(tr3, C.POINTER(C.POINTER(C.POINTER(Track)))),
+                 tracks=C.cast(C.c_void_p(tr3.ctypes.data), C.POINTER(C.POINTER(C.POINTER(Track)))),
                  sources=C.cast(sources, C.POINTER(Source)), polar_angles=polar.ctypes.data_as(fp),
                  leakage=C.cast(leak, fp),
                  expTable=Table(values=table.ctypes.data_as(fp), dx=hp.table_dx,
