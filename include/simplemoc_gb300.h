@@ -38,7 +38,7 @@ extern "C" {
 #define MOC_ERR_OOM          3  /* device allocation failed                    */
 #define MOC_ERR_STATE        4  /* call out of order / handle not usable       */
 #define MOC_ERR_TIMEOUT      5  /* a bounded device wait gave up               */
-#define MOC_ERR_UNSUPPORTED  6  /* mode or size not supported by this build    */
+#define MOC_ERR_UNSUPPORTED  6  /* mode or size not supported by the library  */
 #define MOC_ERR_NO_DEVICE    7  /* no CUDA device visible                      */
 
 /* ---- sweep arithmetic modes (moc_set_mode) ----------------------------- */

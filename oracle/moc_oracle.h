@@ -1,8 +1,8 @@
 /*
  * moc_oracle.h -- CPU oracle for the SimpleMOC transport-sweep path.
  *
- * TEST INFRASTRUCTURE ONLY.  This is the checker that the GPU library is
- * compared against; nothing in the product links, loads or calls it.  Only
+ * TEST INFRASTRUCTURE ONLY.  The GPU library's results are compared against
+ * it; nothing in the product links, loads or calls it.  Only
  * tests/, __graft_entry__.smoke() and the CPU-baseline legs of bench.py use it.
  *
  * It restates, in plain C99, the arithmetic of the reference solver

@@ -10,7 +10,7 @@ if str(ROOT) not in sys.path:
 
 
 def pytest_configure(config):
-    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (runs on the GB300 box)")
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300)")
     config.addinivalue_line("markers", "slow: long-running (full-size workloads)")
 
 
