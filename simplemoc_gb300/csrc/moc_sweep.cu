@@ -287,7 +287,9 @@ __device__ __forceinline__ int checked_source(const SweepArgs &a, int s, int li)
 // CSR: the tracks' segment streams are variable-length (the reference
 // traversal's sub-segments, csr_off/csr_ds/csr_z/csr_src) with the start height
 // of every sub-segment given; otherwise every track has S segments and its
-// height advances by ds*mu.  CSR runs one track per warp (TPW == 32).
+// height advances by ds*mu.  With several CSR tracks in a warp the warp runs
+// to its longest track: the stream shuffles and the geometry stay warp-uniform,
+// and a track past its end skips the arithmetic and the tallies.
 // One 3D track (or one group of TPW lanes' track) of the sweep.  TPW_CT is
 // the threads per track when known at compile time; 0 takes tpw_rt (the
 // batched kernel, where each core has its own width).
@@ -353,12 +355,15 @@ __device__ __forceinline__ void sweep_track(const SweepArgs &a, int64_t track, i
 
   float ds = __shfl_sync(FULL, ds_c, 0, TPW);
   Seg g = segment_geometry(a, z, checked_source(a, __shfl_sync(FULL, src_c, 0, TPW), li));
+  int S_loop = S;                        // the warp's longest track (CSR, several a warp)
+  if (CSR && TPW < 32) S_loop = (int)__reduce_max_sync(FULL, (unsigned)S);
   Rows<CPL, QUAD> rows;
-  if (S > 0) load_rows<CPL, QUAD>(a, g, li, TPW, rows);
+  if (S_loop > 0) load_rows<CPL, QUAD>(a, g, li, TPW, rows);
 
   int ck_left = 0;                       // segments to the next checkpoint
   int64_t ck_slot = CKPT ? tr * a.ck_n : 0;
-  for (int n = 0; n < S; ++n) {
+  for (int n = 0; n < S_loop; ++n) {
+    const bool live = n < S;             // false only past a CSR track's end
     if (CKPT && ck_left-- == 0) {
       // angular flux and height entering segment n (n a multiple of ck_k),
       // for the reverse sweep
@@ -380,7 +385,7 @@ __device__ __forceinline__ void sweep_track(const SweepArgs &a, int64_t track, i
     Seg g1 = g;
     Rows<CPL, QUAD> rows1 = rows;
     const int m = n + 1;
-    if (m < S) {
+    if (m < S_loop) {
       const int k = m & (TPW - 1);
       if (k == 0) {
         ds_c = ds_n;
@@ -403,7 +408,7 @@ __device__ __forceinline__ void sweep_track(const SweepArgs &a, int64_t track, i
 #pragma unroll
     for (int k = 0; k < CPL; ++k) {
       const int c = li + TPW * k;
-      if (c >= a.nchunk) continue;
+      if (c >= a.nchunk || !live) continue;
       const int g4 = 4 * c;
       const float *cf = a.coef + g.crow + 4 * COEF_PLANES * c;    // this chunk's planes
       const float4 sig = __ldg(reinterpret_cast<const float4 *>(cf));
@@ -493,7 +498,6 @@ __global__ void __launch_bounds__(BLOCK) sweep_kernel(SweepArgs a) {
   const int gw = lane / TPW;
   const int64_t warp_id = ((int64_t)blockIdx.x * BLOCK + threadIdx.x) >> 5;
   const int64_t n_warps = ((int64_t)gridDim.x * BLOCK) >> 5;
-  static_assert(!CSR || TPW == 32, "variable-length streams run one track per warp");
   for (int64_t base = warp_id * GPW; base < a.n3d; base += n_warps * GPW)
     sweep_track<TPW, CPL, MODE, QUAD, CSR, CKPT>(a, base + gw, lane, TPW, s_table);
 }
@@ -1225,11 +1229,11 @@ int moc_launch_sweep_csr(moc_problem *p, const int64_t *off, const float *ds, co
   const int nchunk = p->ldg / 4;
   if (p->mode == MOC_MODE_FP64) return MOC_ERR_UNSUPPORTED;
   const bool plain = p->mode == MOC_MODE_PLAIN;
-  if (nchunk <= 32)
-    return plain ? (quad ? launch_t<32, 1, MODE_PLAIN, true, true>(p, a)
-                         : launch_t<32, 1, MODE_PLAIN, false, true>(p, a))
-                 : (quad ? launch_t<32, 1, MODE_MIXED, true, true>(p, a)
-                         : launch_t<32, 1, MODE_MIXED, false, true>(p, a));
+  if (nchunk <= 32)                      // two stacked rays a warp, two chunks a lane
+    return plain ? (quad ? launch_t<16, 2, MODE_PLAIN, true, true>(p, a)
+                         : launch_t<16, 2, MODE_PLAIN, false, true>(p, a))
+                 : (quad ? launch_t<16, 2, MODE_MIXED, true, true>(p, a)
+                         : launch_t<16, 2, MODE_MIXED, false, true>(p, a));
   if (nchunk <= 64)
     return plain ? (quad ? launch_t<32, 2, MODE_PLAIN, true, true>(p, a)
                          : launch_t<32, 2, MODE_PLAIN, false, true>(p, a))
