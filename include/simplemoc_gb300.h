@@ -262,6 +262,14 @@ int moc_openmoc_read(const char *path, int cmfd, int64_t n_tracks_2d, int64_t n_
 int moc_adjoint_forward(moc_problem *p, int k_ckpt);
 int moc_adjoint_backward(moc_problem *p, const float *dphi, float *dq, double *dsigt,
                          float *dpsi_in);
+/* The same, with the fine-source gradient also given per quadratic fit
+ * (src/solver.c:69-81): the segments that fit fine rows w, w+1, w+2 of a source
+ * use q(z) = c0 + c1 z + c2 z^2 with c0 = y2, c1 = (y1 - y3)/(2dz),
+ * c2 = (y1 - 2 y2 + y3)/(2dz^2), and
+ *   dfit [NS][F-2][3][G]   dL/dc0, dL/dc1, dL/dc2 of window w of each source,
+ * summed over those segments.  Quadratic source only (MOC_ERR_UNSUPPORTED). */
+int moc_adjoint_backward_fit(moc_problem *p, const float *dphi, float *dq, double *dsigt,
+                             float *dpsi_in, float *dfit);
 /* Lanes per track (1..32, any width) and 4-group chunks per lane (1 or 2) of
  * the reverse sweep; 0, 0 = automatic (ceil(G/4) lanes of one chunk up to 128
  * groups).  MOC_ERR_ARG when lanes x chunks x 4 < G. */

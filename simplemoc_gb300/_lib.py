@@ -110,6 +110,8 @@ SIGNATURES = {
     "moc_adjoint_backward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                        C.c_void_p]),
     "moc_set_adjoint_width": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "moc_adjoint_backward_fit": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                           C.c_void_p, C.c_void_p]),
     "moc_set_pipeline": (C.c_int, [C.c_void_p, C.c_int]),
     "moc_get_pipeline": (C.c_int, [C.c_void_p, C.POINTER(C.c_int)]),
     "moc_openmoc_probe": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(C.c_int32),

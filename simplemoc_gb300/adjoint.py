@@ -71,6 +71,22 @@ def sweep(q: torch.Tensor, sigma_t: torch.Tensor, solver: Solver, k_ckpt: int = 
     return TransportSweep.apply(q, sigma_t, solver, k_ckpt)
 
 
+def fit_gradients(solver: Solver, dphi: torch.Tensor) -> torch.Tensor:
+    """dL/d(c0, c1, c2) of each quadratic source fit (src/solver.c:69-81) for
+    dL/dphi, after a forward sweep with checkpoints (TransportSweep.forward or
+    moc_adjoint_forward): [NS, F-2, 3, G], window w fitting fine rows w, w+1,
+    w+2 of a source.  Quadratic source only."""
+    s = solver.spec
+    dphi = dphi.detach().to(torch.float32).contiguous()
+    out = torch.empty((s.n_sources, s.fai - 2, 3, s.n_groups), dtype=torch.float32,
+                      device=dphi.device)
+    _sync_torch(dphi.device)
+    L.check(solver._lib.moc_adjoint_backward_fit(solver.handle, dphi.data_ptr(), None, None, None,
+                                                 out.data_ptr()), "moc_adjoint_backward_fit")
+    solver.synchronize()
+    return out
+
+
 class FixedSourceLoss:
     """Loss of the adjoint workload as a function of (sigma_t, S, nu*SigmaF, phi0)."""
 

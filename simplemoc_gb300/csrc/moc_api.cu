@@ -260,7 +260,7 @@ void release(moc_problem *p) {
   dfree(p->psi_b64); dfree(p->partials); dfree(p->scalars); dfree(p->err);
   dfree(p->xs_order); dfree(p->upd_items); dfree(p->psi_scale); dfree(p->psi_b_nonzero);
   dfree(p->ck_psi); dfree(p->ck_z); dfree(p->adj_dphi); dfree(p->adj_dq); dfree(p->adj_dsig);
-  dfree(p->tc_b); dfree(p->tc_items);
+  dfree(p->tc_b); dfree(p->tc_items); dfree(p->adj_dfit);
   if (p->ev0) cudaEventDestroy(p->ev0);
   if (p->ev1) cudaEventDestroy(p->ev1);
   if (p->copy_stream) cudaStreamSynchronize(p->copy_stream);
@@ -901,11 +901,12 @@ int moc_adjoint_forward(moc_problem *p, int k_ckpt) {
   return MOC_OK;
 }
 
-int moc_adjoint_backward(moc_problem *p, const float *dphi, float *dq, double *dsigt,
-                         float *dpsi_in) {
+int moc_adjoint_backward_fit(moc_problem *p, const float *dphi, float *dq, double *dsigt,
+                             float *dpsi_in, float *dfit) {
   int rc = ready(p);
   if (rc != MOC_OK) return rc;
   if (!dphi || !p->ck_psi) return !dphi ? MOC_ERR_ARG : MOC_ERR_STATE;
+  if (dfit && p->d.axial_exp != 2) return MOC_ERR_UNSUPPORTED;   // no fit for a flat source
   cudaSetDevice(p->device);
   const int64_t G = p->d.n_groups;
   if (!p->adj_dphi) {
@@ -914,20 +915,34 @@ int moc_adjoint_backward(moc_problem *p, const float *dphi, float *dq, double *d
     if (rc == MOC_OK) rc = dalloc(p, &p->adj_dsig, (int64_t)p->d.n_sigt * p->ldg);
     if (rc != MOC_OK) return rc;
   }
+  const int64_t fit_rows = p->d.n_sources * (int64_t)(p->d.fai - 2) * 3;
+  if (dfit && !p->adj_dfit) {
+    rc = dalloc(p, &p->adj_dfit, fit_rows * p->ldg);
+    if (rc != MOC_OK) return rc;
+  }
   const size_t fb = sizeof(float) * (size_t)(p->nfsr * p->ldg);
   MOC_CUDA_TRY(cudaMemsetAsync(p->adj_dphi, 0, fb, p->stream));
   MOC_CUDA_TRY(cudaMemsetAsync(p->adj_dq, 0, fb, p->stream));
   MOC_CUDA_TRY(cudaMemsetAsync(p->adj_dsig, 0, sizeof(double) * (size_t)p->d.n_sigt * p->ldg,
                                p->stream));
+  if (dfit)
+    MOC_CUDA_TRY(cudaMemsetAsync(p->adj_dfit, 0, sizeof(float) * (size_t)(fit_rows * p->ldg),
+                                 p->stream));
   rc = copy_rows_dd(p, p->adj_dphi, p->ldg, dphi, G, p->nfsr, G);
   if (rc == MOC_OK)
     rc = moc_launch_adjoint(p, p->ck_psi, p->ck_z, p->ck_k, p->ck_n, p->adj_dphi, p->adj_dq,
-                            p->adj_dsig, dpsi_in);
+                            p->adj_dsig, dpsi_in, dfit ? p->adj_dfit : nullptr);
   if (rc == MOC_OK && dq) rc = copy_rows_dd(p, dq, G, p->adj_dq, p->ldg, p->nfsr, G);
   if (rc == MOC_OK && dsigt)
     rc = copy_rows_dd(p, dsigt, G, p->adj_dsig, p->ldg, (int64_t)p->d.n_sigt, G);
+  if (rc == MOC_OK && dfit) rc = copy_rows_dd(p, dfit, G, p->adj_dfit, p->ldg, fit_rows, G);
   if (rc != MOC_OK) return fail(p, rc);
   return MOC_OK;
+}
+
+int moc_adjoint_backward(moc_problem *p, const float *dphi, float *dq, double *dsigt,
+                         float *dpsi_in) {
+  return moc_adjoint_backward_fit(p, dphi, dq, dsigt, dpsi_in, nullptr);
 }
 
 }  // extern "C"

@@ -94,6 +94,7 @@ struct moc_problem {
   // tensor-core update_sources (MIXED): per material the split operand
   // [hi, lo][tc_np x tc_kp] in the canonical layout, and tiles of <= 128 / F
   // sources of one material (material, first, end) in xs_order
+  float *adj_dfit = nullptr;            // [NS][F-2][3][ldg] fit-coefficient adjoints
   float *tc_b = nullptr;
   int32_t *tc_items = nullptr;
   int32_t n_tc_items = 0;
@@ -169,7 +170,7 @@ int moc_launch_sweep_batch(int device, cudaStream_t st, int mode, bool quad, con
 int moc_reset_psi_scale(moc_problem *p);
 int moc_launch_sweep_ckpt(moc_problem *p, float *ck_psi, float *ck_z, int k, int nck);
 int moc_launch_adjoint(moc_problem *p, const float *ck_psi, const float *ck_z, int k, int nck,
-                       const float *dphi, float *dq, double *dsig, float *dpsi_in);
+                       const float *dphi, float *dq, double *dsig, float *dpsi_in, float *dfit);
 int moc_sweep_launch_shape(const moc_problem *p, int *tpw, int *cpl);
 int moc_sweep_autotune(moc_problem *p, int64_t n_sub, int *tpw, int *cpl, int *stages,
                        double *ms);

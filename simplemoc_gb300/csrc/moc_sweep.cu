@@ -1299,6 +1299,7 @@ struct AdjArgs {
   float *dq;              // [NS*F*ldg] dL/dq, added to
   double *dsig;           // [n_sigt*ldg] dL/dsigma_t, added to
   float *dpsi_in;         // [N3D*G] dL/dpsi entering each track, or null
+  float *dfit;            // [NS][F-2][3][ldg] dL/d(c0, c1, c2) per fit window, or null
   int n_sigt;
   int slices;             // 1: shared-memory accumulators per sub-warp
   int tpw;                // lanes per track (any width 1..32)
@@ -1307,6 +1308,7 @@ struct AdjArgs {
 
 struct AdjOut {
   float pbar, y1b, y2b, y3b, sbar;
+  float c0b, c1b, c2b;    // quadratic source: dL/d of the fit's c0, c1, c2
 };
 
 __device__ __forceinline__ AdjOut adj_quad(const SweepArgs &a, float y1, float y2, float y3,
@@ -1334,6 +1336,9 @@ __device__ __forceinline__ AdjOut adj_quad(const SweepArgs &a, float y1, float y
   o.y1b = c1b * a.rd1 + c2b * a.rd2;
   o.y2b = q0b - 2.f * c2b * a.rd2;
   o.y3b = c2b * a.rd2 - c1b * a.rd1;
+  o.c0b = q0b;                                        // q0 = c0 + c1 zin + c2 zin^2
+  o.c1b = c1b;
+  o.c2b = c2b;
   const float A = (q0 * tau + (sig * psi - q0) * e) * r2;
   const float dA = (q0 * ds + psi * e + (sig * psi - q0) * eps * ds) * r2 - 2.f * A * r1;
   const float dR = (2.f * tau - 2.f) * ds + 2.f * eps * ds * r3 - 6.f * e * r3 * r1;
@@ -1354,6 +1359,7 @@ __device__ __forceinline__ AdjOut adj_flat(float y, float sig, float r1, float d
   o.pbar = pbar + dbar * e;
   o.y1b = -dbar * e * r1;
   o.y2b = o.y3b = 0.f;
+  o.c0b = o.c1b = o.c2b = 0.f;
   o.sbar = dbar * (y * r1 * r1 * e + (psi - y * r1) * eps * ds);
   return o;
 }
@@ -1512,7 +1518,7 @@ __global__ void __launch_bounds__(BLOCK, 2) adjoint_kernel(AdjArgs x) {
           if (c >= a.nchunk) continue;
           const int g4 = 4 * c;
           const float4 ph = hist_base[(jj * CPL + k) * BLOCK];
-          float4 b1, b2, b3, sb;
+          float4 b1, b2, b3, sb, f0, f1, f2;
 #pragma unroll
           for (int e = 0; e < 4; ++e) {
             const float abar = get(cur.lam[k], e) * (QUAD ? w : w_mu);
@@ -1528,6 +1534,9 @@ __global__ void __launch_bounds__(BLOCK, 2) adjoint_kernel(AdjArgs x) {
             set(b2, e, o.y2b);
             set(b3, e, o.y3b);
             set(sb, e, g4 + e < a.G ? o.sbar : 0.f);
+            set(f0, e, o.c0b);
+            set(f1, e, o.c1b);
+            set(f2, e, o.c2b);
           }
           if (valid) {
             if (acc) {
@@ -1551,6 +1560,15 @@ __global__ void __launch_bounds__(BLOCK, 2) adjoint_kernel(AdjArgs x) {
             if (QUAD) {
               red_add_v4(dq + a.ldg, b2.x, b2.y, b2.z, b2.w);
               red_add_v4(dq + 2 * a.ldg, b3.x, b3.y, b3.z, b3.w);
+              if (x.dfit) {
+                // the fit window: its first row r0 of source s (rows s F + r0 ..)
+                const int64_t wrow = g.qrow / a.ldg;
+                const int64_t src = wrow / a.F, r0 = wrow - src * a.F;
+                float *df = x.dfit + ((src * (a.F - 2) + r0) * 3) * a.ldg + g4;
+                red_add_v4(df, f0.x, f0.y, f0.z, f0.w);
+                red_add_v4(df + a.ldg, f1.x, f1.y, f1.z, f1.w);
+                red_add_v4(df + 2 * a.ldg, f2.x, f2.y, f2.z, f2.w);
+              }
             }
           }
         }
@@ -1647,7 +1665,7 @@ int moc_launch_sweep_ckpt(moc_problem *p, float *ck_psi, float *ck_z, int k, int
 }
 
 int moc_launch_adjoint(moc_problem *p, const float *ck_psi, const float *ck_z, int k, int nck,
-                       const float *dphi, float *dq, double *dsig, float *dpsi_in) {
+                       const float *dphi, float *dq, double *dsig, float *dpsi_in, float *dfit) {
   if (k < 1 || k > ADJ_KMAX) return MOC_ERR_ARG;
   AdjArgs x{};
   x.a = build_args(p);
@@ -1660,6 +1678,7 @@ int moc_launch_adjoint(moc_problem *p, const float *ck_psi, const float *ck_z, i
   x.dq = dq;
   x.dsig = dsig;
   x.dpsi_in = dpsi_in;
+  x.dfit = dfit;
   x.n_sigt = p->d.n_sigt;
   return p->d.axial_exp == 2 ? dispatch_adj<true>(p, x) : dispatch_adj<false>(p, x);
 }

@@ -207,3 +207,49 @@ def test_adjoint_time_within_three_forward_sweeps(gpu_available):
     print(f"forward sweep {t_fwd:.2f} ms, adjoint {times[best]:.2f} ms (forward with "
           f"checkpoints {parts[best][0]:.2f} + reverse {parts[best][1]:.2f}), ratio {ratio:.2f}")
     assert ratio <= 3.0
+
+
+def test_adjoint_fit_coefficient_gradients(gpu_available):
+    """dL/d(c0, c1, c2) per fit window (src/solver.c:69-81), mapped back through
+    c0 = y2, c1 = (y1 - y3)/(2dz), c2 = (y1 - 2 y2 + y3)/(2dz^2), give the
+    kernel's dL/d fine_source (<= 1e-5 normwise: FP32 sums in other orders);
+    a flat source has no fit."""
+    import torch
+
+    import simplemoc_gb300 as sm
+    L = _lib()
+    spec = sm.ProblemSpec(n_groups=12, fai=5, cai=4, height=200.0, n_sources=60, n_tracks_2d=12,
+                          n_polar=4, z_stacked=10, n_seg=50, seed=31)
+    hp = sm.generate(spec)
+    G, F, NS = spec.n_groups, spec.fai, spec.n_sources
+    dev = torch.device("cuda", 0)
+    dphi = torch.from_numpy(np.random.default_rng(4).random(NS * F * G).astype(np.float32)).to(dev)
+    with sm.Solver(hp, mode="mixed") as s:
+        lib, h = s._lib, s.handle
+        L.check(lib.moc_zero_state(h, 1, 1), "zero")
+        L.check(lib.moc_adjoint_forward(h, 8), "fwd")
+        dq = torch.empty(NS * F * G, dtype=torch.float32, device=dev)
+        dfit = torch.empty(NS * (F - 2) * 3 * G, dtype=torch.float32, device=dev)
+        torch.cuda.synchronize()
+        L.check(lib.moc_adjoint_backward_fit(h, dphi.data_ptr(), dq.data_ptr(), None, None,
+                                             dfit.data_ptr()), "bwd_fit")
+        s.synchronize()
+    dz = np.float32(spec.height) / np.float32(F * spec.decomp_ax * spec.cai)
+    rd1 = np.float64(np.float32(1.0) / (np.float32(2.0) * dz))
+    rd2 = np.float64(np.float32(1.0) / (np.float32(2.0) * dz * dz))
+    fit = dfit.cpu().numpy().astype(np.float64).reshape(NS, F - 2, 3, G)
+    back = np.zeros((NS, F, G))
+    c0, c1, c2 = fit[:, :, 0], fit[:, :, 1], fit[:, :, 2]
+    back[:, 0:F - 2] += c1 * rd1 + c2 * rd2
+    back[:, 1:F - 1] += c0 - 2.0 * c2 * rd2
+    back[:, 2:F] += c2 * rd2 - c1 * rd1
+    ref = dq.cpu().numpy().astype(np.float64).reshape(NS, F, G)
+    assert np.abs(ref).max() > 0 and np.abs(fit).max() > 0
+    assert np.abs(back - ref).max() / np.abs(ref).max() <= 1e-5
+    flat = sm.generate(spec.with_(axial_exp=0))
+    with sm.Solver(flat, mode="mixed") as s:
+        lib, h = s._lib, s.handle
+        L.check(lib.moc_adjoint_forward(h, 8), "fwd")
+        torch.cuda.synchronize()
+        rc = lib.moc_adjoint_backward_fit(h, dphi.data_ptr(), None, None, None, dfit.data_ptr())
+        assert rc == 6          # MOC_ERR_UNSUPPORTED
