@@ -68,6 +68,21 @@ def _dist():
     return rank, world, local
 
 
+def _job_value(ms_local: float, units_per_step: float, steps: int, world: int, pg,
+               device: str = "cuda") -> tuple[float, float]:
+    """The whole job's time and throughput: every rank runs its own replica
+    (weak scaling), the job takes as long as the slowest rank, and the value
+    counts the units of all ranks.  pg is torch.distributed (any backend) or
+    None for one process."""
+    ms = ms_local
+    if pg is not None:
+        import torch
+        t = torch.tensor([ms], dtype=torch.float64, device=device)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms, world * units_per_step * steps / (ms / 1e3)
+
+
 def _peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -467,12 +482,7 @@ def main():
         r = solver.time_power_iterations(K)
     launches = solver.launch_count() - l0
     barrier()
-    ms = r["ms_total"]
-    if pg:
-        t = torch.tensor([ms], device="cuda")
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * ints * K / (ms / 1e3)
+    ms, value = _job_value(r["ms_total"], ints, K, world, pg)
     sweep_ms = r["ms_sweeps"] / K
 
     # ---- plain (reference arithmetic) ------------------------------------------
