@@ -231,6 +231,30 @@ int moc_zero_state(moc_problem *p, int flux, int psi);
 int moc_get_fine_flux_device(moc_problem *p, float *phi);
 int moc_get_fine_flux64_device(moc_problem *p, double *phi);   /* FP64 mode */
 
+/* ---- failure handling ---------------------------------------------------
+ * Every call returns a status; after a CUDA failure, or after a kernel found an
+ * invalid input or a bounded device wait ran out (reported by the next call
+ * that waits for the device: MOC_ERR_ARG / MOC_ERR_TIMEOUT), the handle's status
+ * is sticky and later calls return MOC_ERR_STATE.  Other handles and the CUDA
+ * context stay usable: no kernel of the library traps.
+ *
+ * moc_set_memory_limit caps the device bytes one handle may allocate (0: no
+ * cap; allocations beyond it are MOC_ERR_OOM, e.g. to keep several handles
+ * inside a budget or to test out-of-memory handling).
+ * moc_inject_fault marks a handle as a failing call would (host side, for
+ * tests of a caller's error handling):
+ *   MOC_FAULT_CUDA            a failed CUDA call (status MOC_ERR_CUDA, sticky)
+ *   MOC_FAULT_DEVICE_INPUT    a kernel's input check (next wait: MOC_ERR_ARG)
+ *   MOC_FAULT_DEVICE_TIMEOUT  a bounded device wait (next wait: MOC_ERR_TIMEOUT)
+ * moc_selftest_wait runs a kernel whose wait nothing completes, bounded by
+ * `cycles` SM clocks (1 .. 2^32): it returns MOC_ERR_TIMEOUT. */
+#define MOC_FAULT_CUDA           0
+#define MOC_FAULT_DEVICE_INPUT   1
+#define MOC_FAULT_DEVICE_TIMEOUT 2
+int moc_set_memory_limit(int64_t bytes);
+int moc_inject_fault(moc_problem *p, int kind);
+int moc_selftest_wait(moc_problem *p, int64_t cycles);
+
 /* ---- OpenMOC track files (src/tracks.c:170-323, the reference's -d input) --
  * moc_openmoc_probe reads the sizes of a track file; moc_openmoc_read fills
  * caller arrays sized from them (any output may be NULL):

@@ -26,6 +26,9 @@ MOC_MODE_MIXED = 1
 MOC_MODE_FP64 = 2
 MOC_FLAG_COMPENSATED = 0x1
 MOC_FLAG_SIMT_UPDATE = 0x2
+MOC_FAULT_CUDA = 0
+MOC_FAULT_DEVICE_INPUT = 1
+MOC_FAULT_DEVICE_TIMEOUT = 2
 
 f32p = C.POINTER(C.c_float)
 f64p = C.POINTER(C.c_double)
@@ -110,6 +113,9 @@ SIGNATURES = {
     "moc_adjoint_backward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                        C.c_void_p]),
     "moc_set_adjoint_width": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "moc_set_memory_limit": (C.c_int, [C.c_int64]),
+    "moc_inject_fault": (C.c_int, [C.c_void_p, C.c_int]),
+    "moc_selftest_wait": (C.c_int, [C.c_void_p, C.c_int64]),
     "moc_adjoint_backward_fit": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                            C.c_void_p, C.c_void_p]),
     "moc_set_pipeline": (C.c_int, [C.c_void_p, C.c_int]),

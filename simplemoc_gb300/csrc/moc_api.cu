@@ -7,10 +7,12 @@
 #include <stdint.h>
 #include <string.h>
 
+#include <atomic>
 #include <new>
 #include <vector>
 
 #include "moc_host.h"
+
 #include "moc_internal.h"
 
 namespace {
@@ -29,9 +31,14 @@ __global__ void fold_kernel(float *__restrict__ hi, float *__restrict__ lo, int6
   }
 }
 
+// Device bytes one handle may allocate (0: no limit); moc_set_memory_limit.
+std::atomic<int64_t> g_memory_limit{0};
+
 template <typename T>
 int dalloc(moc_problem *p, T **ptr, int64_t count) {
   if (count <= 0) count = 1;
+  const int64_t limit = g_memory_limit.load();
+  if (limit > 0 && p->bytes + (int64_t)sizeof(T) * count > limit) return MOC_ERR_OOM;
   void *d = nullptr;
   cudaError_t e = cudaMalloc(&d, sizeof(T) * (size_t)count);
   if (e != cudaSuccess) {
@@ -349,6 +356,31 @@ int sweep_impl(moc_problem *p) {
 
 }  // namespace
 
+// A device wait that nothing completes: an mbarrier expecting one arrival
+// that never comes, polled with the same clock-bounded loop as every device
+// wait of the library; on expiry it sets the timeout bit and returns.
+__global__ void selftest_wait_kernel(int32_t *err, long long cycles) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x != 0) return;
+  const uint32_t addr = (uint32_t)__cvta_generic_to_shared(&bar);
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(addr), "r"(1) : "memory");
+  const long long t0 = clock64();
+  for (;;) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred P1;\n\tmbarrier.try_wait.parity.shared::cta.b64 P1, [%1], %2;\n\t"
+        "selp.b32 %0, 1, 0, P1;\n\t}\n"
+        : "=r"(done)
+        : "r"(addr), "r"(0)
+        : "memory");
+    if (done) return;
+    if (clock64() - t0 > cycles) {
+      atomicOr(err, 2);
+      return;
+    }
+  }
+}
+
 int moc_join_upload(moc_problem *p) {
   if (p->n_chunks == 0) return MOC_OK;
   p->n_chunks = 0;
@@ -361,6 +393,42 @@ int moc_join_upload(moc_problem *p) {
 }
 
 extern "C" {
+
+int moc_selftest_wait(moc_problem *p, int64_t cycles) {
+  int rc = ready(p);
+  if (rc != MOC_OK) return rc;
+  if (cycles < 1 || cycles > (int64_t)1 << 32) return MOC_ERR_ARG;   // at most ~2 s
+  cudaSetDevice(p->device);
+  selftest_wait_kernel<<<1, 32, 0, p->stream>>>(p->err, (long long)cycles);
+  if (cudaGetLastError() != cudaSuccess) return fail(p, MOC_ERR_CUDA);
+  p->launches++;
+  return sync_check(p);
+}
+
+int moc_set_memory_limit(int64_t bytes) {
+  if (bytes < 0) return MOC_ERR_ARG;
+  g_memory_limit.store(bytes);
+  return MOC_OK;
+}
+
+int moc_inject_fault(moc_problem *p, int kind) {
+  if (!p) return MOC_ERR_ARG;
+  cudaSetDevice(p->device);
+  switch (kind) {
+    case MOC_FAULT_CUDA:                  // as if a CUDA call of the handle had failed
+      fail(p, MOC_ERR_CUDA);
+      return MOC_OK;
+    case MOC_FAULT_DEVICE_INPUT:          // a kernel found an invalid source id
+    case MOC_FAULT_DEVICE_TIMEOUT: {      // a bounded device wait ran out
+      const int32_t bit = kind == MOC_FAULT_DEVICE_INPUT ? 1 : 2;
+      MOC_CUDA_TRY(cudaMemcpyAsync(p->err, &bit, sizeof bit, cudaMemcpyHostToDevice, p->stream));
+      MOC_CUDA_TRY(cudaStreamSynchronize(p->stream));
+      return MOC_OK;
+    }
+    default:
+      return MOC_ERR_ARG;
+  }
+}
 
 const char *moc_status_string(int status) {
   switch (status) {
