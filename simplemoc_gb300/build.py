@@ -65,7 +65,7 @@ def build(verbose: bool = False) -> Path:
         obj = BUILD / (src + ".o")
         objs.append(obj)
         if _stale(obj, [CSRC / src] + headers):
-            jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fopenmp",
+            jobs.append(["g++", "-O3", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fopenmp",
                          *inc, "-c", str(CSRC / src), "-o", str(obj)])
     with ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
         for cmd in jobs:

@@ -102,6 +102,56 @@ int put(moc_problem *p, T *dst, const T *src, int64_t count, cudaStream_t st = n
     if (rc_ != MOC_OK) return rc_;  \
   } while (0)
 
+// Host staging of the arrays the upload derives: one pinned block per handle,
+// allocated on the first upload, so that their copies are asynchronous (a copy
+// from pageable memory first waits for everything queued on its stream, here
+// the 2 GB of fine source and flux).  An event recorded after the last copy
+// from the block guards its reuse by the next upload.
+struct Staging {
+  float *seg_ds, *weight, *mu, *coef, *st, *tc_b;
+  int32_t *order, *items, *tc_items;
+};
+
+int staging(moc_problem *p, Staging *out) {
+  const moc_dims &d = p->d;
+  const int64_t G = d.n_groups, NS = d.n_sources;
+  const int64_t n[9] = {
+      (int64_t)d.n_tracks_2d * d.n_polar * d.n_seg,                 // seg_ds
+      p->n3d,                                                       // weight
+      d.n_polar,                                                    // mu
+      (int64_t)d.n_sigt * COEF_PLANES * p->ldg,                     // coef
+      (int64_t)d.n_xs * G * G,                                      // st
+      p->tc_b ? (int64_t)d.n_xs * 2 * p->tc_np * p->tc_kp : 0,      // tc_b
+      NS,                                                           // order
+      3 * ((int64_t)d.n_xs + NS / 128 + 1),                         // items
+      p->tc_b ? 3 * ((int64_t)d.n_xs + NS / (128 / d.fai) + 1) : 0  // tc_items
+  };
+  size_t off[10] = {0};
+  for (int i = 0; i < 9; ++i) off[i + 1] = off[i] + ((size_t)n[i] * 4 + 63) / 64 * 64;
+  if (!p->h_stage) {
+    if (cudaMallocHost(&p->h_stage, off[9]) != cudaSuccess) {
+      cudaGetLastError();
+      p->h_stage = nullptr;
+      return MOC_ERR_OOM;
+    }
+    MOC_CUDA_TRY(cudaEventCreateWithFlags(&p->stage_ev, cudaEventDisableTiming));
+  } else if (p->stage_pending) {
+    MOC_CUDA_TRY(cudaEventSynchronize(p->stage_ev));
+  }
+  p->stage_pending = false;
+  unsigned char *b = static_cast<unsigned char *>(p->h_stage);
+  out->seg_ds = reinterpret_cast<float *>(b + off[0]);
+  out->weight = reinterpret_cast<float *>(b + off[1]);
+  out->mu = reinterpret_cast<float *>(b + off[2]);
+  out->coef = reinterpret_cast<float *>(b + off[3]);
+  out->st = reinterpret_cast<float *>(b + off[4]);
+  out->tc_b = reinterpret_cast<float *>(b + off[5]);
+  out->order = reinterpret_cast<int32_t *>(b + off[6]);
+  out->items = reinterpret_cast<int32_t *>(b + off[7]);
+  out->tc_items = reinterpret_cast<int32_t *>(b + off[8]);
+  return MOC_OK;
+}
+
 // Uploads every input and state array of `h` (validated) into the storage.
 // With stream_tracks the per-track arrays go on the copy stream in chunks of
 // whole 2D tracks (events chunk_ev[k]) and the call returns with the upload in
@@ -113,23 +163,17 @@ int upload_all(moc_problem *p, const moc_host *h, bool stream_tracks) {
   if (stream_tracks) {
     // Fine source and flux (2 GB on the default problem) go first, so that the
     // host's validation and derivation below run while they are in flight; the
-    // per-track arrays follow on the copy stream at the end.  The copy stream
-    // waits for the work already queued on the stream (a sweep may still read
-    // the arrays it overwrites).  The arrays copied before the validation must
-    // at least exist.
+    // per-track arrays follow on the copy stream at the end.  The arrays copied
+    // before the validation must at least exist.
     if (!h->fine_source || !h->seg_src) return MOC_ERR_ARG;
-    MOC_CUDA_TRY(cudaEventRecord(p->main_ev, p->stream));
-    MOC_CUDA_TRY(cudaStreamWaitEvent(p->copy_stream, p->main_ev, 0));
     TRY(put_rows(p, p->q, h->fine_source, p->nfsr));
     TRY(put_rows(p, p->phi, h->fine_flux, p->nfsr));
     TRY(moc_host_validate_except_ids(&d, h));   // the ids chunk by chunk, below
   }
-  std::vector<float> seg_ds((size_t)(N2D * P * S)), mu((size_t)P), weight((size_t)p->n3d);
-  std::vector<float> coef((size_t)d.n_sigt * COEF_PLANES * p->ldg);
-  std::vector<float> st((size_t)d.n_xs * G * G);
+  Staging sg;
+  TRY(staging(p, &sg));
   float max_step = 0.0f;
-  TRY(moc_host_derive(&d, h, p->ldg, seg_ds.data(), mu.data(), weight.data(), coef.data(),
-                      st.data(), &max_step));
+  TRY(moc_host_derive(&d, h, p->ldg, sg.seg_ds, sg.mu, sg.weight, sg.coef, sg.st, &max_step));
   // one wrap per segment keeps the height rule exact (checked, not assumed)
   const float hd = d.height / (float)d.decomp_ax;
   if (!(max_step < hd)) return MOC_ERR_ARG;
@@ -150,52 +194,54 @@ int upload_all(moc_problem *p, const moc_host *h, bool stream_tracks) {
     }
     p->fmagic = m;
   }
-  TRY(put(p, p->seg_ds, seg_ds.data(), N2D * P * S));
+  TRY(put(p, p->seg_ds, sg.seg_ds, N2D * P * S));
   if (!stream_tracks) TRY(put(p, p->seg_src, h->seg_src, p->n3d * S));
-  TRY(put(p, p->weight, weight.data(), p->n3d));
+  TRY(put(p, p->weight, sg.weight, p->n3d));
   TRY(put(p, p->z0, h->z0, p->n3d));
-  TRY(put(p, p->mu, mu.data(), P));
+  TRY(put(p, p->mu, sg.mu, P));
   TRY(put(p, p->src_sigt, h->src_sigt, NS));
   TRY(put(p, p->src_xs, h->src_xs, NS));
   TRY(put(p, p->vol, h->vol, NS));
-  TRY(put(p, p->coef, coef.data(), (int64_t)coef.size()));
+  TRY(put(p, p->coef, sg.coef, (int64_t)d.n_sigt * COEF_PLANES * p->ldg));
   TRY(put(p, p->xs, h->xs, (int64_t)d.n_xs * G * 3));
-  TRY(put(p, p->scatter_t, st.data(), (int64_t)st.size()));
+  TRY(put(p, p->scatter_t, sg.st, (int64_t)d.n_xs * G * G));
   TRY(put(p, p->table, h->table, 2 * (int64_t)d.table_n));
   // update_sources work list: sources grouped by xs row, items of <= 128 sources
   {
     std::vector<int64_t> start((size_t)d.n_xs + 1, 0);
     for (int64_t s = 0; s < NS; ++s) start[(size_t)h->src_xs[s] + 1]++;
     for (int32_t m = 0; m < d.n_xs; ++m) start[(size_t)m + 1] += start[(size_t)m];
-    std::vector<int32_t> order((size_t)NS), items;
+    int32_t *order = sg.order, *items = sg.items;
+    int64_t n_items = 0;
     std::vector<int64_t> fill(start.begin(), start.end() - 1);
     for (int64_t s = 0; s < NS; ++s) order[(size_t)fill[(size_t)h->src_xs[s]]++] = (int32_t)s;
     for (int32_t m = 0; m < d.n_xs; ++m)
       for (int64_t a = start[(size_t)m]; a < start[(size_t)m + 1]; a += 128) {
         const int64_t b = a + 128 < start[(size_t)m + 1] ? a + 128 : start[(size_t)m + 1];
-        items.push_back(m);
-        items.push_back((int32_t)a);
-        items.push_back((int32_t)b);
+        items[n_items++] = m;
+        items[n_items++] = (int32_t)a;
+        items[n_items++] = (int32_t)b;
       }
-    p->n_upd_items = (int32_t)(items.size() / 3);
-    TRY(put(p, p->xs_order, order.data(), NS));
-    TRY(put(p, p->upd_items, items.data(), (int64_t)items.size()));
+    p->n_upd_items = (int32_t)(n_items / 3);
+    TRY(put(p, p->xs_order, order, NS));
+    TRY(put(p, p->upd_items, items, n_items));
     // tensor-core tiles: <= 128 fine regions (128 / F sources) of one material,
     // and per material the split second operand (scatter rows, nuSigmaF, SigmaA)
-    std::vector<int32_t> tc_items;
-    std::vector<float> tc_b;
     if (p->tc_b) {
       const int64_t per = 128 / d.fai;
+      int32_t *tc_items = sg.tc_items;
+      int64_t n_tc = 0;
       for (int32_t m = 0; m < d.n_xs; ++m)
         for (int64_t a = start[(size_t)m]; a < start[(size_t)m + 1]; a += per) {
           const int64_t b = a + per < start[(size_t)m + 1] ? a + per : start[(size_t)m + 1];
-          tc_items.push_back(m);
-          tc_items.push_back((int32_t)a);
-          tc_items.push_back((int32_t)b);
+          tc_items[n_tc++] = m;
+          tc_items[n_tc++] = (int32_t)a;
+          tc_items[n_tc++] = (int32_t)b;
         }
       const int kp = p->tc_kp, np = p->tc_np;
       const int64_t plane = (int64_t)np * kp;
-      tc_b.assign((size_t)(d.n_xs * 2 * plane), 0.0f);
+      float *tc_b = sg.tc_b;
+      std::memset(tc_b, 0, sizeof(float) * (size_t)(d.n_xs * 2 * plane));
       for (int64_t m = 0; m < d.n_xs; ++m)
         for (int n = 0; n < G + 2; ++n)
           for (int k = 0; k < G; ++k) {
@@ -206,12 +252,13 @@ int upload_all(moc_problem *p, const moc_host *h, bool stream_tracks) {
             tc_b[(size_t)o] = hi;
             tc_b[(size_t)(o + plane)] = moc_tf32_rna(v - hi);
           }
-      p->n_tc_items = (int32_t)(tc_items.size() / 3);
-      TRY(put(p, p->tc_items, tc_items.data(), (int64_t)tc_items.size()));
-      TRY(put(p, p->tc_b, tc_b.data(), (int64_t)tc_b.size()));
+      p->n_tc_items = (int32_t)(n_tc / 3);
+      TRY(put(p, p->tc_items, tc_items, n_tc));
+      TRY(put(p, p->tc_b, tc_b, d.n_xs * 2 * plane));
     }
-    // the pageable sources above must be consumed before the vectors go away
-    MOC_CUDA_TRY(cudaStreamSynchronize(p->stream));
+    // the staged sources are reused by the next upload once these copies ran
+    MOC_CUDA_TRY(cudaEventRecord(p->stage_ev, p->stream));
+    p->stage_pending = true;
   }
   if (!stream_tracks) {
     TRY(put_rows(p, p->q, h->fine_source, p->nfsr));
@@ -220,8 +267,12 @@ int upload_all(moc_problem *p, const moc_host *h, bool stream_tracks) {
     TRY(put_rows(p, p->psi_f, h->psi_f, p->n3d));
     TRY(put_rows(p, p->psi_b, h->psi_b, p->n3d));
   } else {
-    // the per-track arrays last: the host-to-device copies run in issue order,
-    // and the small arrays above are what the first chunk's sweep waits for
+    // the per-track arrays last, after everything queued on the stream: copies
+    // on two streams share the copy engines, and the fine source, flux and
+    // derived arrays above are what the first chunk's sweep waits for (this also
+    // orders the chunks after any sweep still reading the arrays they overwrite)
+    MOC_CUDA_TRY(cudaEventRecord(p->main_ev, p->stream));
+    MOC_CUDA_TRY(cudaStreamWaitEvent(p->copy_stream, p->main_ev, 0));
     const int n = (int)(N2D < moc_problem::MAX_UPLOAD_CHUNKS ? N2D : moc_problem::MAX_UPLOAD_CHUNKS);
     const int64_t PZ = P * d.z_stacked;
     for (int k = 0; k < n; ++k) {
@@ -268,6 +319,11 @@ void release(moc_problem *p) {
   dfree(p->xs_order); dfree(p->upd_items); dfree(p->psi_scale); dfree(p->psi_b_nonzero);
   dfree(p->ck_psi); dfree(p->ck_z); dfree(p->adj_dphi); dfree(p->adj_dq); dfree(p->adj_dsig);
   dfree(p->tc_b); dfree(p->tc_items); dfree(p->adj_dfit);
+  if (p->stage_ev) cudaEventSynchronize(p->stage_ev);
+  if (p->h_stage) cudaFreeHost(p->h_stage);
+  if (p->stage_ev) cudaEventDestroy(p->stage_ev);
+  p->h_stage = nullptr;
+  p->stage_ev = nullptr;
   if (p->ev0) cudaEventDestroy(p->ev0);
   if (p->ev1) cudaEventDestroy(p->ev1);
   if (p->copy_stream) cudaStreamSynchronize(p->copy_stream);

@@ -240,11 +240,11 @@ void moc_host_coef(const moc_dims *d, const float *sigt, int32_t ldg, float *coe
 
 int moc_host_validate_ids(const moc_dims *d, const moc_host *h, int64_t first, int64_t end) {
   const int64_t NS = d->n_sources;
-  const int32_t *ids = h->seg_src;
-  int bad = 0;
-#pragma omp parallel for schedule(static) reduction(| : bad)
-  for (int64_t k = first; k < end; k++) bad |= (ids[k] < 0 || ids[k] >= NS);
-  return bad ? MOC_ERR_ARG : MOC_OK;
+  const uint32_t *ids = reinterpret_cast<const uint32_t *>(h->seg_src);
+  uint32_t mx = 0;                       // a negative id is a huge unsigned one
+#pragma omp parallel for schedule(static) reduction(max : mx)
+  for (int64_t k = first; k < end; k++) mx = ids[k] > mx ? ids[k] : mx;
+  return end > first && (int64_t)mx >= NS ? MOC_ERR_ARG : MOC_OK;
 }
 
 int moc_host_validate(const moc_dims *d, const moc_host *h) {

@@ -123,6 +123,9 @@ struct moc_problem {
   int n_chunks = 0;
   bool detect_pending = false;                   // psi_b's nonzero flag still to be set
   bool stale = false;                            // an upload was rejected: device state undefined
+  void *h_stage = nullptr;                       // pinned host staging of derived arrays
+  cudaEvent_t stage_ev = nullptr;                // after the last copy from h_stage
+  bool stage_pending = false;
   // host copies needed for re-upload and derived arrays
   float polar[64];
 };
