@@ -1,7 +1,12 @@
 """Benchmark: segment-group integrations/s of the SimpleMOC transport sweep.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--config default|small]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--config CONFIG] [--launch T,C]
     python bench.py --impl reference ...     # the CPU reference arm
+
+CONFIG: default (the headline), batched (64 independent cores in one launch,
+CUDA-graph power iteration), adjoint (adjoint / forward sweep time), dropin
+(power iterations through the reference's own entry points), small and
+default_1k (parity and profiling sizes).
 
 A step is one power iteration of src/main.c:57-92 (transport sweep,
 renormalize_flux, update_sources, compute_keff) over the whole problem; the
@@ -14,7 +19,8 @@ synthetic and seeded, larger than L2 (no flush needed).
 `value` is the chosen mode (MIXED: the fastest mode whose FSR flux stays
 within 1e-5 of the FP64 mode); the PLAIN (reference-arithmetic) rate is
 reported beside it.  `e2e` repeats the measurement through the public C ABI
-with pinned host buffers: every step uploads all inputs, runs one power
+with pinned host buffers: every step uploads all inputs (streamed: the sweep
+starts on the first chunks of tracks while the rest copy), runs one power
 iteration and downloads the FSR fluxes and k_eff.
 
 With --gpus N > 1 (torchrun) every rank sweeps an independent replica of the
