@@ -13,8 +13,9 @@
 // the main product Ahi.Bhi is accumulated in up to three K ranges, each in its
 // own tensor-memory accumulator, and the two correction products in a fourth;
 // the epilogue adds the four with FP32 round-to-nearest (the accumulation bias
-// drops from ~1.4e-6 to the level of the CUDA-core kernel).  The epilogue (one thread per
-// region row and half of its columns) forms the new source
+// drops from ~1.4e-6 to the level of the CUDA-core kernel).  Four threads per
+// region row read its accumulator columns into shared memory; the epilogue,
+// coalesced along the rows, forms the new source
 //     q = (nuSigmaF.phi / k * chi + S phi) / (4 pi)
 // with the residual and the k_eff partial sums, as update_tiled_kernel does.
 //
@@ -31,7 +32,7 @@
 namespace {
 
 constexpr int TC_M = 128;          // fine regions per tile = tensor-memory lanes
-constexpr int TC_THREADS = 256;    // two threads per region row
+constexpr int TC_THREADS = 512;    // four threads per region row
 constexpr int TC_MAX_KG = 26;      // K groups of 4 (groups <= 104)
 constexpr double TC_PI = 3.14159265358979323846;
 // ~1 s at 2 GHz: an MMA tile takes microseconds, so only a fault of the
@@ -105,8 +106,8 @@ __device__ __forceinline__ void tc_fence_after() {
 }
 
 // 16 columns of the product: the main-product accumulators in K order, then
-// the corrections (at 3 * stride), added in FP32 round-to-nearest.  All loads
-// are issued before the one wait.
+// the corrections (at 3 * stride), added in FP32 round-to-nearest as
+// ((K0 + K1) + K2) + corrections.
 __device__ __forceinline__ void tmem_ld16_nowait(uint32_t taddr, uint32_t (&r)[16]) {
   asm volatile(
       "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,"
@@ -119,21 +120,18 @@ __device__ __forceinline__ void tmem_ld16_nowait(uint32_t taddr, uint32_t (&r)[1
 
 __device__ __forceinline__ void acc_ld16(uint32_t taddr, uint32_t stride, int n_chain,
                                          float (&v)[16]) {
-  uint32_t ra[16], rb[16];
-  tmem_ld16_nowait(taddr, ra);                      // K range 0
-  if (n_chain > 1) tmem_ld16_nowait(taddr + stride, rb);   // K range 1
+  uint32_t r[16];
+  tmem_ld16_nowait(taddr, r);                       // K range 0
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-  for (int i = 0; i < 16; ++i)
-    v[i] = n_chain > 1 ? __fadd_rn(__uint_as_float(ra[i]), __uint_as_float(rb[i]))
-                       : __uint_as_float(ra[i]);
-  if (n_chain > 2) tmem_ld16_nowait(taddr + 2 * stride, ra);   // K range 2
-  tmem_ld16_nowait(taddr + 3 * stride, rb);                    // corrections
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+  // K ranges 1 and 2, then the corrections, in that order
+  for (int c = 1; c <= 3; ++c) {
+    if (c < 3 && c >= n_chain) continue;
+    tmem_ld16_nowait(taddr + (uint32_t)c * stride, r);
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
-  for (int i = 0; i < 16; ++i) {
-    if (n_chain > 2) v[i] = __fadd_rn(v[i], __uint_as_float(ra[i]));
-    v[i] = __fadd_rn(v[i], __uint_as_float(rb[i]));
+    for (int i = 0; i < 16; ++i) v[i] = __fadd_rn(v[i], __uint_as_float(r[i]));
   }
 }
 
@@ -191,10 +189,11 @@ __device__ __forceinline__ int64_t tile_grow(const TcArgs &x, int it, int row) {
   return (int64_t)x.xs_order[s0 + row / x.F] * x.F + row % x.F;
 }
 
-// Each warp moves 16 rows of a tile as (row, K group) pairs, lane-consecutive
-// along the row: element e = lane + 32 t of warp w is row 16 w + e / kgroups,
+// Each warp moves 8 rows of a tile as (row, K group) pairs, lane-consecutive
+// along the row: element e = lane + 32 t of warp w is row 8 w + e / kgroups,
 // K group e % kgroups.  rk[t] packs (row << 8) | kgroup, -1 past the warp's rows.
-constexpr int TC_PER_LANE = (16 * TC_MAX_KG + 31) / 32;   // 13
+constexpr int TC_ROWS_PER_WARP = TC_M / (TC_THREADS / 32);            // 8
+constexpr int TC_PER_LANE = (TC_ROWS_PER_WARP * TC_MAX_KG + 31) / 32;   // 7
 
 __global__ void __launch_bounds__(TC_THREADS, 1) update_tc_kernel(TcArgs x) {
   extern __shared__ __align__(128) unsigned char tc_smem[];
@@ -204,7 +203,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) update_tc_kernel(TcArgs x) {
   __shared__ double sh[TC_THREADS / 32];
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int row = tid & (TC_M - 1);            // = (warp % 4) * 32 + lane: its TMEM lane
-  const int half = tid >> 7;                   // 0: first half of the accumulator columns
+  const int part = tid >> 7;                   // which quarter of the accumulator columns
   const int KP = x.kp, NP = x.np, G = x.G, ldg = x.ldg;
   const int kgroups = KP / 4;
   const int DS = NP + 4;                       // accumulator row stride in shared memory
@@ -220,7 +219,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1) update_tc_kernel(TcArgs x) {
 #pragma unroll
   for (int t = 0; t < TC_PER_LANE; ++t) {
     const int e = lane + 32 * t;
-    rk[t] = e < 16 * kgroups ? ((16 * warp + e / kgroups) << 8) | (e % kgroups) : -1;
+    rk[t] = e < TC_ROWS_PER_WARP * kgroups
+                ? ((TC_ROWS_PER_WARP * warp + e / kgroups) << 8) | (e % kgroups)
+                : -1;
   }
 
   if (warp == 0) {
@@ -257,8 +258,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) update_tc_kernel(TcArgs x) {
   uint32_t phase = 0;
   int cur_m = -1;
   const int nch = (NP + 15) / 16;               // 16-column chunks of the product
-  const int ch_split = (nch + 1) / 2;
-  const int c0 = half ? ch_split : 0, c1 = half ? nch : ch_split;
+  const int c0 = part * nch / 4, c1 = (part + 1) * nch / 4;
 
   // this tile's fluxes, coalesced: row-consecutive 16-byte pieces per lane
   float4 buf[TC_PER_LANE];
@@ -351,9 +351,9 @@ __global__ void __launch_bounds__(TC_THREADS, 1) update_tc_kernel(TcArgs x) {
     phase ^= 1u;
     tc_fence_after();
     // ---- the accumulator rows to shared memory (A is consumed), one thread
-    // per row and half of its 16-column chunks
+    // per row and a quarter of its 16-column chunks
 #pragma unroll
-    for (int cc = 0; cc < 4; ++cc) {
+    for (int cc = 0; cc < (MOC_TC_MAX_NP / 16 + 3) / 4; ++cc) {
       const int c = c0 + cc;
       if (c >= c1) break;                      // the same on every lane of a warp
       float v[16];
@@ -381,6 +381,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1) update_tc_kernel(TcArgs x) {
       const float4 d4 = *reinterpret_cast<const float4 *>(d_s + r * DS + g);
       const float fk = __fmul_rn(d_s[r * DS + G], inverse_k);
       const float *pd = &d4.x;
+      const float4 chi4 = *reinterpret_cast<const float4 *>(chi_s + g);   // one conflict-free read
+      const float *pc = &chi4.x;
       const float4 old = qold[t];
       float4 nw = old;
       const float *po = &old.x;
@@ -389,7 +391,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) update_tc_kernel(TcArgs x) {
       for (int e = 0; e < 4; ++e) {
         if (g + e >= G) continue;
         // src/solver.c:1289-1295
-        const float num = __fadd_rn(__fmul_rn(fk, chi_s[g + e]), pd[e]);
+        const float num = __fadd_rn(__fmul_rn(fk, pc[e]), pd[e]);
         float qq = __fmul_rn(num, r_four_pi);
         qq = __fmaf_rn(__fmaf_rn(-qq, four_pi, num), r_four_pi, qq);
         pn[e] = qq;
