@@ -143,15 +143,18 @@ int moc_create(const moc_dims *dims, const moc_host *host, int device,
 int moc_destroy(moc_problem *p);
 /* Re-uploads every input array of `host` into the existing storage (same
  * dims).  The per-track arrays (seg_src, psi_f, psi_b) are copied on a second
- * stream in up to 8 chunks of whole 2D tracks and the call returns with them
- * in flight: the next moc_transport_sweep / moc_power_iteration sweeps each
- * chunk as soon as it lands, and every other call waits for the copies first.
- * The host arrays must stay unchanged until a call that waits for the device
- * (moc_synchronize, moc_download, moc_power_iteration with outputs, ...) has
- * returned.  The host validates the input while the copies run; invalid input
- * (e.g. a source id out of range) is MOC_ERR_ARG, after the call has let its
- * copies finish, and then every other call returns MOC_ERR_STATE until an
- * upload succeeds (the device state is partly overwritten). */
+ * stream in up to 8 chunks of whole 2D tracks (the first 1/256 of them, each
+ * next chunk 4x the one before) and the call returns with them in flight: the
+ * next moc_transport_sweep / moc_power_iteration sweeps each chunk as soon as
+ * it lands, and every other call waits for the copies first.  The host arrays
+ * must stay unchanged until a call that waits for the device (moc_synchronize,
+ * moc_download, moc_power_iteration with outputs, ...) has returned.
+ * Invalid input is MOC_ERR_ARG: from this call for everything but the
+ * per-segment source ids, which the sweep checks as it reads them (an id out
+ * of range is swept as source 0); the first call after that sweep that waits
+ * for the device returns MOC_ERR_ARG.  Either way every other call then
+ * returns MOC_ERR_STATE until an upload succeeds (the device state is partly
+ * overwritten); the handle itself stays usable for that upload. */
 int moc_upload(moc_problem *p, const moc_host *host);
 /* Copies results back (any pointer may be NULL to skip that array). */
 int moc_download(moc_problem *p, float *fine_flux, float *fine_source,

@@ -164,11 +164,14 @@ int upload_all(moc_problem *p, const moc_host *h, bool stream_tracks) {
     // Fine source and flux (2 GB on the default problem) go first, so that the
     // host's validation and derivation below run while they are in flight; the
     // per-track arrays follow on the copy stream at the end.  The arrays copied
-    // before the validation must at least exist.
+    // before the validation must at least exist.  The per-segment source ids
+    // (2.6 GB) are not scanned on the host: the sweep reads every id through a
+    // bounds check (MOC_DEV_ERR_SOURCE), so the upload returns in a few ms and
+    // the first sweep starts as soon as the first chunk has landed.
     if (!h->fine_source || !h->seg_src) return MOC_ERR_ARG;
     TRY(put_rows(p, p->q, h->fine_source, p->nfsr));
     TRY(put_rows(p, p->phi, h->fine_flux, p->nfsr));
-    TRY(moc_host_validate_except_ids(&d, h));   // the ids chunk by chunk, below
+    TRY(moc_host_validate_except_ids(&d, h));
   }
   Staging sg;
   TRY(staging(p, &sg));
@@ -273,18 +276,18 @@ int upload_all(moc_problem *p, const moc_host *h, bool stream_tracks) {
     // orders the chunks after any sweep still reading the arrays they overwrite)
     MOC_CUDA_TRY(cudaEventRecord(p->main_ev, p->stream));
     MOC_CUDA_TRY(cudaStreamWaitEvent(p->copy_stream, p->main_ev, 0));
-    const int n = (int)(N2D < moc_problem::MAX_UPLOAD_CHUNKS ? N2D : moc_problem::MAX_UPLOAD_CHUNKS);
     const int64_t PZ = P * d.z_stacked;
-    for (int k = 0; k < n; ++k) {
-      const int64_t i0 = N2D * k / n, i1 = N2D * (k + 1) / n;
+    int n = 0;
+    int64_t len = N2D / 256 > 0 ? N2D / 256 : 1;
+    for (int64_t i1 = 0; i1 < N2D; ++n, len *= 4) {
+      const int64_t i0 = i1;
+      i1 = (n == moc_problem::MAX_UPLOAD_CHUNKS - 1 || N2D - i0 <= len) ? N2D : i0 + len;
       const int64_t t0 = i0 * PZ, nt = (i1 - i0) * PZ;
-      // this chunk's source ids are checked while the previous chunk copies
-      TRY(moc_host_validate_ids(&d, h, t0 * S, (t0 + nt) * S));
       TRY(put(p, p->seg_src + t0 * S, h->seg_src + t0 * S, nt * S, p->copy_stream));
       TRY(put_rows(p, p->psi_f + t0 * p->ldg, h->psi_f ? h->psi_f + t0 * G : nullptr, nt,
                    p->copy_stream));
-      MOC_CUDA_TRY(cudaEventRecord(p->chunk_ev[k], p->copy_stream));
-      p->chunk_end[k] = i1;
+      MOC_CUDA_TRY(cudaEventRecord(p->chunk_ev[n], p->copy_stream));
+      p->chunk_end[n] = i1;
     }
     TRY(put_rows(p, p->psi_b, h->psi_b, p->n3d, p->copy_stream));
     MOC_CUDA_TRY(cudaEventRecord(p->copy_done, p->copy_stream));
@@ -367,7 +370,11 @@ int sync_check(moc_problem *p) {
   int32_t err = 0;
   e = cudaMemcpy(&err, p->err, sizeof(int32_t), cudaMemcpyDeviceToHost);
   if (e != cudaSuccess) return fail(p, MOC_ERR_CUDA);
-  if (err & 2) return fail(p, MOC_ERR_TIMEOUT);   // a bounded device wait gave up
+  if (err & MOC_DEV_ERR_TIMEOUT) return fail(p, MOC_ERR_TIMEOUT);
+  if (err == MOC_DEV_ERR_SOURCE) {   // input of the last upload: refuse work until the next
+    p->stale = true;
+    return MOC_ERR_ARG;
+  }
   if (err != 0) return fail(p, MOC_ERR_ARG);
   return MOC_OK;
 }
@@ -431,7 +438,7 @@ __global__ void selftest_wait_kernel(int32_t *err, long long cycles) {
         : "memory");
     if (done) return;
     if (clock64() - t0 > cycles) {
-      atomicOr(err, 2);
+      atomicOr(err, MOC_DEV_ERR_TIMEOUT);
       return;
     }
   }
@@ -595,7 +602,8 @@ int moc_upload(moc_problem *p, const moc_host *host) {
   int rc = moc_join_upload(p);
   if (rc != MOC_OK) return fail(p, rc);
   // FP64 state is widened from the uploaded FP32 state at once: no streaming.
-  // Streamed uploads validate while their copies are in flight.
+  // Streamed uploads validate all but the per-segment source ids while their
+  // copies are in flight; the sweep checks the ids (MOC_DEV_ERR_SOURCE).
   const bool streamed = p->q64 == nullptr;
   if (!streamed) {
     rc = moc_host_validate(&p->d, host);

@@ -11,6 +11,10 @@
 
 #include <vector>
 
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
 #include "moc_host.h"
 #include "simplemoc_gb300.h"
 
@@ -238,19 +242,37 @@ void moc_host_coef(const moc_dims *d, const float *sigt, int32_t ldg, float *coe
   }
 }
 
-int moc_host_validate_ids(const moc_dims *d, const moc_host *h, int64_t first, int64_t end) {
+int moc_host_validate_ids(const moc_dims *d, const int32_t *seg_src, int64_t first, int64_t end) {
   const int64_t NS = d->n_sources;
-  const uint32_t *ids = reinterpret_cast<const uint32_t *>(h->seg_src);
+  const uint32_t *ids = reinterpret_cast<const uint32_t *>(seg_src);
   uint32_t mx = 0;                       // a negative id is a huge unsigned one
-#pragma omp parallel for schedule(static) reduction(max : mx)
-  for (int64_t k = first; k < end; k++) mx = ids[k] > mx ? ids[k] : mx;
-  return end > first && (int64_t)mx >= NS ? MOC_ERR_ARG : MOC_OK;
+  // One contiguous block per thread, eight independent maxima per step (two
+  // 4-lane vector maxima): the scan runs at memory speed rather than at the
+  // latency of one dependent max per id.
+  constexpr int W = 8;
+  const int64_t n = end > first ? end - first : 0;
+#pragma omp parallel reduction(max : mx)
+  {
+    int nt = 1, t = 0;
+#ifdef _OPENMP
+    nt = omp_get_num_threads();
+    t = omp_get_thread_num();
+#endif
+    const int64_t a = first + n * t / nt, b = first + n * (t + 1) / nt;
+    uint32_t m[W] = {0};
+    int64_t k = a;
+    for (; k + W <= b; k += W)
+      for (int j = 0; j < W; ++j) m[j] = ids[k + j] > m[j] ? ids[k + j] : m[j];
+    for (; k < b; ++k) m[0] = ids[k] > m[0] ? ids[k] : m[0];
+    for (int j = 0; j < W; ++j) mx = m[j] > mx ? m[j] : mx;
+  }
+  return n > 0 && (int64_t)mx >= NS ? MOC_ERR_ARG : MOC_OK;
 }
 
 int moc_host_validate(const moc_dims *d, const moc_host *h) {
   int rc = moc_host_validate_except_ids(d, h);
   if (rc != MOC_OK) return rc;
-  return moc_host_validate_ids(d, h, 0,
+  return moc_host_validate_ids(d, h->seg_src, 0,
                                d->n_tracks_2d * d->n_polar * d->z_stacked * (int64_t)d->n_seg);
 }
 

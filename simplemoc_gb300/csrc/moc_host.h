@@ -9,7 +9,7 @@ int moc_host_validate(const moc_dims *d, const moc_host *h);
 // The same checks in two parts: all but the per-segment source ids, and the
 // source ids k in [first, end) of seg_src.
 int moc_host_validate_except_ids(const moc_dims *d, const moc_host *h);
-int moc_host_validate_ids(const moc_dims *d, const moc_host *h, int64_t first, int64_t end);
+int moc_host_validate_ids(const moc_dims *d, const int32_t *seg_src, int64_t first, int64_t end);
 // Builds the derived arrays the kernels read: 3D segment lengths per
 // (2D track, polar, segment), cos(theta) per polar angle, the track weights,
 // the sigma_t coefficient planes, and the transposed scatter table.

@@ -108,7 +108,7 @@ struct moc_problem {
   // reductions / scalars
   double *partials = nullptr;    // [3 * RED_BLOCKS]
   double *scalars = nullptr;     // see post kernels
-  int32_t *err = nullptr;
+  int32_t *err = nullptr;        // device error word, MOC_DEV_ERR_* bits
   int32_t red_blocks = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   // Upload of the per-track arrays (segment sources, psi_f, psi_b) on a copy
@@ -122,13 +122,22 @@ struct moc_problem {
   int64_t chunk_end[MAX_UPLOAD_CHUNKS] = {};     // one past the chunk's last 2D track
   int n_chunks = 0;
   bool detect_pending = false;                   // psi_b's nonzero flag still to be set
-  bool stale = false;                            // an upload was rejected: device state undefined
+  bool stale = false;                            // rejected input: device state undefined
   void *h_stage = nullptr;                       // pinned host staging of derived arrays
   cudaEvent_t stage_ev = nullptr;                // after the last copy from h_stage
   bool stage_pending = false;
   // host copies needed for re-upload and derived arrays
   float polar[64];
 };
+
+// Bits of the device error word.  A source id out of range comes from the
+// input of the last upload (a streamed upload leaves the ids to the sweep,
+// which reads each one through a bounds check that substitutes source 0): the
+// handle then refuses work until the next valid upload, where the other bits
+// are failures of the handle.
+constexpr int32_t MOC_DEV_ERR_ARG = 1;        // an argument error found by a kernel
+constexpr int32_t MOC_DEV_ERR_TIMEOUT = 2;    // a bounded device wait gave up
+constexpr int32_t MOC_DEV_ERR_SOURCE = 4;     // a segment source id out of range
 
 // Launchers implemented in moc_sweep.cu / moc_post.cu.
 int moc_launch_sweep(moc_problem *p);

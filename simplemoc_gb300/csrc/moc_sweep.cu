@@ -296,8 +296,8 @@ __device__ __forceinline__ void load_rows(const SweepArgs &a, const Seg &g, int 
 }
 
 __device__ __forceinline__ int checked_source(const SweepArgs &a, int s, int li) {
-  if ((uint32_t)s >= (uint64_t)a.ns) {   // validated at upload; never trusted blindly
-    if (li == 0) atomicOr(a.err, 1);
+  if ((uint32_t)s >= (uint64_t)a.ns) {   // the ids of a streamed upload are checked here
+    if (li == 0) atomicOr(a.err, MOC_DEV_ERR_SOURCE);
     return 0;
   }
   return s;
@@ -861,7 +861,7 @@ __global__ void __launch_bounds__(BLOCK) sweep64_kernel(SweepArgs a) {
       const float dsf = __ldg(dsb + n);
       int s = __ldg(srcb + n);
       if ((uint32_t)s >= (uint64_t)a.ns) {
-        if (li == 0) atomicOr(a.err, 1);
+        if (li == 0) atomicOr(a.err, MOC_DEV_ERR_SOURCE);
         s = 0;
       }
       const double ds = dsf;

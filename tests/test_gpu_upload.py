@@ -7,7 +7,7 @@ the synchronous upload at creation gives:
 * fine_flux: FP32 atomic tallies in another order, normwise <= 1e-5;
 * k_eff and the renormalised psi_b: <= 1e-5 relative.
 
-13 2D tracks make eight uneven chunks (one or two 2D tracks each).
+13 2D tracks make three chunks of 1, 4 and 8 2D tracks (the chunks grow 4x).
 """
 import ctypes as C
 
@@ -97,23 +97,64 @@ def test_upload_round_trip_and_ordering(gpu_available):
     assert np.array_equal(ra["psi_f"], rb["psi_f"])
 
 
-def test_upload_rejects_bad_source_ids(gpu_available):
-    import simplemoc_gb300 as sm
-    hp = _problem(seed=10)
+def _bad_ids(hp, track_2d):
+    """A copy of the state whose first segment of 2D track `track_2d` has a
+    source id out of range."""
     bad = hp.copy_state()
     bad.seg_src = hp.seg_src.copy()
-    bad.seg_src[hp.seg_src.size // 2] = hp.spec.n_sources
-    with sm.Solver(hp, mode="plain") as b:
-        with pytest.raises(sm.MocError):
-            b.upload(bad)
-        # the rejected upload overwrote part of the state: work is refused ...
-        with pytest.raises(sm.MocError):
-            b.transport_sweep()
-        # ... until a valid upload, after which the handle sweeps as a fresh one
-        b.upload(hp)
-        b.transport_sweep()
-        out = b.download(psi_f=True, fine_flux=False, fine_source=False)
+    spec = hp.spec
+    bad.seg_src[track_2d * spec.n_polar * spec.z_stacked * spec.n_seg] = spec.n_sources
+    return bad
+
+
+def _fresh_sweep_matches(b, hp):
+    """After a valid upload the handle sweeps as a fresh one."""
+    import simplemoc_gb300 as sm
+    b.upload(hp)
+    b.transport_sweep()
+    out = b.download(psi_f=True, fine_flux=False, fine_source=False)
     with sm.Solver(hp, mode="plain") as a:
         a.transport_sweep()
         ref = a.download(psi_f=True, fine_flux=False, fine_source=False)
     assert np.array_equal(out["psi_f"], ref["psi_f"])
+
+
+MOC_ERR_ARG, MOC_ERR_STATE = 1, 4
+
+
+@pytest.mark.parametrize("track_2d", [0, 12])          # the first and the last chunk
+@pytest.mark.parametrize("then", ["sweep_download", "power_iteration", "upload"])
+def test_bad_source_ids_are_reported_by_the_next_waiting_call(gpu_available, track_2d, then):
+    """A streamed upload leaves the source ids to the sweep, which reads each
+    one through a bounds check: an id out of range makes the next call that
+    waits for the device return MOC_ERR_ARG, then work is refused until a valid
+    upload (a second upload before any sweep simply replaces the first)."""
+    import simplemoc_gb300 as sm
+    hp = _problem(seed=10)
+    with sm.Solver(hp, mode="plain") as b:
+        b.upload(_bad_ids(hp, track_2d))
+        if then == "upload":
+            _fresh_sweep_matches(b, hp)
+            return
+        with pytest.raises(sm.MocError) as e:
+            if then == "sweep_download":
+                b.transport_sweep()
+                b.download(psi_f=True, fine_flux=False, fine_source=False)
+            else:
+                b.power_iteration(1.0)
+        assert e.value.status == MOC_ERR_ARG
+        with pytest.raises(sm.MocError) as e:
+            b.transport_sweep()
+        assert e.value.status == MOC_ERR_STATE
+        assert b._lib.moc_status(b.handle) == 0          # refused, not failed
+        _fresh_sweep_matches(b, hp)
+
+
+def test_create_rejects_bad_source_ids(gpu_available):
+    """Creation uploads synchronously and checks every id on the host."""
+    import simplemoc_gb300 as sm
+    hp = _problem(seed=10)
+    bad = _bad_ids(hp, 12)
+    with pytest.raises(sm.MocError) as e:
+        sm.Solver(bad, mode="plain")
+    assert e.value.status == MOC_ERR_ARG
