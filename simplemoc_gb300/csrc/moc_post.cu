@@ -42,33 +42,62 @@ __device__ __forceinline__ double block_sum(double v, double *sh) {
 
 // ---- renormalize_flux, step 1: fission-rate partials, sum of phi*vol*nuSigF
 // (src/solver.c:1160-1175; the float products keep the reference order).  One
-// warp per fine region; each lane adds its groups in FP32 and folds the result
-// into its FP64 accumulator once per region (FP64 arithmetic is a small
-// fraction of FP32 throughput on this part, so it is kept per region, not per
-// element).
+// warp per source: its F fine regions are contiguous rows, and the material's
+// nuSigmaF of the lane's groups is loaded once for all of them (up to 128
+// groups in registers).  Each lane adds its groups of a region in FP32 and
+// folds the result into its FP64 accumulator once per region (FP64 arithmetic
+// is a small fraction of FP32 throughput on this part, so it is kept per
+// region, not per element).
 template <typename T>
 __global__ void __launch_bounds__(RTHREADS) renorm_partials(const T *__restrict__ phi,
-                                                            const float *__restrict__ vol,
-                                                            const int32_t *__restrict__ src_xs,
-                                                            const float *__restrict__ xs,
-                                                            int64_t nfsr, int F, int G, int ldg,
-                                                            double *__restrict__ partials) {
+                                                           const float *__restrict__ vol,
+                                                           const int32_t *__restrict__ src_xs,
+                                                           const float *__restrict__ xs,
+                                                           int64_t ns, int F, int G, int ldg,
+                                                           double *__restrict__ partials) {
   __shared__ double sh[RTHREADS / 32];
   double acc = 0.0;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  for (int64_t row = (int64_t)blockIdx.x * (RTHREADS / 32) + warp; row < nfsr;
-       row += (int64_t)gridDim.x * (RTHREADS / 32)) {
-    const int64_t s = row / F;
+  for (int64_t s = (int64_t)blockIdx.x * (RTHREADS / 32) + warp; s < ns;
+       s += (int64_t)gridDim.x * (RTHREADS / 32)) {
     const float v_s = vol[s];
     const float *x = xs + (int64_t)src_xs[s] * G * 3;
-    const T *ph = phi + row * ldg;
-    if (sizeof(T) == 4) {
-      float r = 0.f;
-      for (int g = lane; g < G; g += 32)
-        r = __fadd_rn(r, __fmul_rn(__fmul_rn((float)ph[g], v_s), x[g * 3 + 0]));
-      acc += (double)r;
+    const T *ph = phi + s * F * ldg;
+    if (G <= 128) {
+      float nsf[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) nsf[i] = lane + 32 * i < G ? __ldg(x + (lane + 32 * i) * 3) : 0.f;
+#pragma unroll 4
+      for (int f = 0; f < F; ++f) {
+        const T *row = ph + (int64_t)f * ldg;
+        if (sizeof(T) == 4) {
+          float r = 0.f;
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            const int g = lane + 32 * i;
+            if (g < G) r = __fadd_rn(r, __fmul_rn(__fmul_rn((float)__ldg(row + g), v_s), nsf[i]));
+          }
+          acc += (double)r;
+        } else {
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            const int g = lane + 32 * i;
+            if (g < G) acc += (double)__ldg(row + g) * (double)v_s * (double)nsf[i];
+          }
+        }
+      }
     } else {
-      for (int g = lane; g < G; g += 32) acc += (double)ph[g] * (double)v_s * (double)x[g * 3];
+      for (int f = 0; f < F; ++f) {
+        const T *row = ph + (int64_t)f * ldg;
+        if (sizeof(T) == 4) {
+          float r = 0.f;
+          for (int g = lane; g < G; g += 32)
+            r = __fadd_rn(r, __fmul_rn(__fmul_rn((float)row[g], v_s), x[g * 3 + 0]));
+          acc += (double)r;
+        } else {
+          for (int g = lane; g < G; g += 32) acc += (double)row[g] * (double)v_s * (double)x[g * 3];
+        }
+      }
     }
   }
   double b = block_sum(acc, sh);
@@ -293,8 +322,8 @@ template <typename T>
 int renorm_t(moc_problem *p, T *phi, T *psi_f, T *psi_b, T *adjust) {
   const moc_dims &d = p->d;
   renorm_partials<T><<<RBLOCKS, RTHREADS, 0, p->stream>>>(phi, p->vol, p->src_xs, p->xs,
-                                                          p->nfsr, d.fai, d.n_groups, p->ldg,
-                                                          p->partials);
+                                                          d.n_sources, d.fai, d.n_groups,
+                                                          p->ldg, p->partials);
   renorm_finalize<T><<<1, 32, 0, p->stream>>>(p->partials, RBLOCKS, p->scalars);
   const int64_t ns = d.n_sources;
   renorm_adjust<T><<<(unsigned)((ns + 255) / 256), 256, 0, p->stream>>>(p->vol, ns, d.fai,
@@ -658,8 +687,8 @@ extern "C" int moc_renormalize_flux_noalloc(float *fine_flux, float *psi_f, floa
   // RBLOCKS partials, both scalars, adjust[0..n_sources)), so nothing has to be
   // cleared between calls.  Two calls whose kernels overlap on the GPU (other
   // streams, other host threads) share the one array and race.
-  renorm_partials<float><<<RBLOCKS, RTHREADS, 0, s>>>(fine_flux, vol, src_xs, xs, nfsr, fai,
-                                                      n_groups, n_groups, partials);
+  renorm_partials<float><<<RBLOCKS, RTHREADS, 0, s>>>(fine_flux, vol, src_xs, xs, n_sources,
+                                                      fai, n_groups, n_groups, partials);
   renorm_finalize<float><<<1, 32, 0, s>>>(partials, RBLOCKS, scalars);
   renorm_adjust<float><<<(unsigned)((n_sources + 255) / 256), 256, 0, s>>>(vol, n_sources, fai,
                                                                            scalars, adjust);
