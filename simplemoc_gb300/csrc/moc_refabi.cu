@@ -57,6 +57,7 @@ struct RefArgs {
   double node_dz;           // node_delta_z
   float sep;                // Input.axial_z_sep
   int64_t ns;
+  uint64_t ns_m;            // floor((2^64 - 1) / ns), for mod_barrett
   float *z;                 // [N3D] stacked-ray heights (pass 0: a scratch copy)
   int32_t *cnt;             // [N3D] pass 0: sub-segments; pass 1: emitted so far
   int64_t *ij_tot;          // [N2D*P]
@@ -73,6 +74,30 @@ __device__ __forceinline__ uint64_t mix64(uint64_t z) {
   z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
   z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
   return z ^ (z >> 31);
+}
+
+// x mod d for d >= 1 by Barrett reduction, given m = floor((2^64 - 1) / d):
+// q = umulhi(x, m) is floor(x / d) or one less (x m / 2^64 lies in
+// (x/d - 1, x/d]), so x - q d is the remainder or the remainder + d.  Exact
+// for every 64-bit x, at a fraction of the cost of a 64-bit division.
+__device__ __forceinline__ uint64_t mod_barrett(uint64_t x, uint64_t d, uint64_t m) {
+  const uint64_t q = __umul64hi(x, m);
+  uint64_t r = x - q * d;
+  if (r >= d) r -= d;
+  return r;
+}
+
+// The source region of the sub-segment drawn q-th in traversal order
+// (src/solver.c:476-483): the reference's rand() value (never negative) modulo
+// the region count, or the counter hash modulo the region count.
+__device__ __forceinline__ int32_t sub_segment_source(const RefArgs &r, int64_t q) {
+  if (r.rng) {
+    const int32_t v = r.rng[q];
+    return v >= 0 ? (int32_t)mod_barrett((uint64_t)v, (uint64_t)r.ns, r.ns_m)
+                  : (int32_t)((int64_t)v % r.ns);
+  }
+  return (int32_t)mod_barrett(mix64(r.hash_key + (uint64_t)q * 0x9E3779B97F4A7C15ull),
+                              (uint64_t)r.ns, r.ns_m);
 }
 
 // One 3D track over one 2D segment: the while loop of src/solver.c:409-524.
@@ -115,13 +140,9 @@ __device__ int track_segment(const RefArgs &r, bool pos, double cos_d, float s_f
       }
     }
     if (EMIT) {
-      const int64_t q = seq + count;
-      const int64_t id = r.rng ? (int64_t)(r.rng[q] % r.ns)
-                               : (int64_t)(mix64(r.hash_key + (uint64_t)q * 0x9E3779B97F4A7C15ull) %
-                                           (uint64_t)r.ns);
       r.sds[slot + count] = ds;
       r.sz[slot + count] = zh;
-      r.ssrc[slot + count] = (int32_t)id;
+      r.ssrc[slot + count] = sub_segment_source(r, seq + count);
     }
     ++count;
     if (last_seg || reset)
@@ -461,6 +482,7 @@ RefArgs make_args(RefState &r, float *z) {
   a.node_dz = r.node_dz;
   a.sep = r.sep;
   a.ns = r.ns;
+  a.ns_m = ~0ull / (uint64_t)r.ns;
   a.z = z;
   a.cnt = r.d_cnt;
   a.ij_tot = r.d_ij_tot;
