@@ -363,8 +363,10 @@ int ready(moc_problem *p) {
   return rc == MOC_OK ? MOC_OK : fail(p, rc);
 }
 
+}  // namespace
+
 // Waits for the stream and folds the device error word into the status.
-int sync_check(moc_problem *p) {
+int moc_sync_check(moc_problem *p) {
   cudaError_t e = cudaStreamSynchronize(p->stream);
   if (e != cudaSuccess) return fail(p, MOC_ERR_CUDA);
   int32_t err = 0;
@@ -378,6 +380,10 @@ int sync_check(moc_problem *p) {
   if (err != 0) return fail(p, MOC_ERR_ARG);
   return MOC_OK;
 }
+
+namespace {
+
+int sync_check(moc_problem *p) { return moc_sync_check(p); }
 
 int read_scalars(moc_problem *p, double *out) {
   int rc = sync_check(p);

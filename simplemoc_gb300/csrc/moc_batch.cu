@@ -130,15 +130,29 @@ int batch_post(moc_batch *b) {
 }
 
 // A core uploaded since the batch last ran: its copies must land (and its
-// stream drain) before the batch stream reads its arrays.
+// stream drain) before the batch stream reads its arrays.  A core that failed
+// or whose last upload was rejected is refused.
 int join_cores(moc_batch *b) {
   for (moc_problem *p : b->cores) {
+    if (p->status != MOC_OK || p->stale) return MOC_ERR_STATE;
     if (p->n_chunks == 0) continue;
     int rc = moc_join_upload(p);
     if (rc != MOC_OK) return rc;
     MOC_CUDA_TRY(cudaStreamSynchronize(p->stream));
   }
   return MOC_OK;
+}
+
+// After the batch stream has drained: every core's device error word, as a
+// call on that core would report it (a source id out of range from a streamed
+// upload leaves that core stale).  The first error, MOC_OK if none.
+int check_cores(moc_batch *b) {
+  int first = MOC_OK;
+  for (moc_problem *p : b->cores) {
+    const int rc = moc_sync_check(p);
+    if (first == MOC_OK) first = rc;
+  }
+  return first;
 }
 
 }  // namespace
@@ -160,7 +174,7 @@ int moc_batch_create(int n, moc_problem *const *problems, moc_batch **out) {
   b->quad = p0->d.axial_exp == 2;
   for (moc_problem *p : b->cores) {
     // one launch: same device, mode, source order and (PLAIN) exponential table
-    if (!p || p->status != MOC_OK || p->device != b->device || p->mode != b->mode ||
+    if (!p || p->status != MOC_OK || p->stale || p->device != b->device || p->mode != b->mode ||
         (p->d.axial_exp == 2) != b->quad || p->ldg > 256 || p->mode == MOC_MODE_FP64 ||
         (p->mode == MOC_MODE_MIXED && (p->flags & MOC_FLAG_COMPENSATED)) ||
         p->d.table_n != p0->d.table_n || p->d.table_dx != p0->d.table_dx ||
@@ -322,7 +336,7 @@ int moc_batch_sweep(moc_batch *b) {
   if (rc == MOC_OK) rc = batch_sweep(b);
   if (rc != MOC_OK) return rc;
   MOC_CUDA_TRY(cudaStreamSynchronize(b->stream));
-  return MOC_OK;
+  return check_cores(b);
 }
 
 // `iters` power iterations of every core: the batched sweep, then each core's
@@ -370,13 +384,15 @@ int moc_batch_power_iterations(moc_batch *b, int iters, int use_graph, double *m
   cudaEventElapsedTime(&ms, b->ev0, b->ev1);
   if (ms_total) *ms_total = ms;
   for (moc_problem *p : b->cores) p->psi_pending = true;   // the last step renormalised
-  return MOC_OK;
+  return check_cores(b);
 }
 
 int moc_batch_results(moc_batch *b, double *keff, double *residual) {
   if (!b) return MOC_ERR_ARG;
   cudaSetDevice(b->device);
   MOC_CUDA_TRY(cudaStreamSynchronize(b->stream));
+  const int rc = check_cores(b);
+  if (rc != MOC_OK) return rc;
   for (size_t c = 0; c < b->cores.size(); ++c) {
     double sc[SC_COUNT];
     MOC_CUDA_TRY(cudaMemcpy(sc, b->cores[c]->scalars, sizeof sc, cudaMemcpyDeviceToHost));

@@ -145,6 +145,10 @@ int moc_launch_sweep(moc_problem *p);
 int moc_launch_sweep_range(moc_problem *p, int64_t i2_begin, int64_t i2_end);
 // Makes the stream wait for an upload in flight (no-op when there is none).
 int moc_join_upload(moc_problem *p);
+// Waits for the handle's stream and folds its device error word into the
+// status: MOC_ERR_ARG with the handle stale for a source id out of range (the
+// input of the last upload), a failure of the handle otherwise.
+int moc_sync_check(moc_problem *p);
 
 // Tensor-core update_sources.  The second operand of tile GEMM for material m
 // is B[n][k] (n < G: scatter S[m][n][k]; n = G: nuSigmaF[m][k]; n = G + 1:

@@ -86,3 +86,38 @@ def test_batch_rejects_mixed_modes(gpu_available):
         Batch([a, b])
     a.close()
     b.close()
+
+
+def test_batch_reports_a_cores_bad_source_id(gpu_available):
+    """A streamed upload leaves the source ids to the sweep: a batch that sweeps
+    a core with an id out of range reports MOC_ERR_ARG for it, the core refuses
+    work until a valid upload, and the other cores are untouched."""
+    import simplemoc_gb300 as sm
+    from simplemoc_gb300.batch import Batch
+    specs = _specs()[:3]
+    hps = [sm.generate(s) for s in specs]
+    solvers = [sm.Solver(h, mode="plain") for h in hps]
+    try:
+        with Batch(solvers) as b:
+            bad = hps[1].copy_state()
+            bad.seg_src = hps[1].seg_src.copy()
+            bad.seg_src[-1] = specs[1].n_sources
+            solvers[1].upload(bad)
+            with pytest.raises(sm.MocError) as e:
+                b.sweep()
+            assert e.value.status == 1                     # MOC_ERR_ARG
+            with pytest.raises(sm.MocError) as e:
+                b.sweep()
+            assert e.value.status == 4                     # MOC_ERR_STATE: core 1 is stale
+            for s in solvers:
+                s.upload()
+            b.sweep()
+        for h, s in zip(hps, solvers):
+            out = s.download(psi_f=True, fine_flux=False, fine_source=False)
+            with sm.Solver(h, mode="plain") as alone:
+                alone.transport_sweep()
+                ref = alone.download(psi_f=True, fine_flux=False, fine_source=False)
+            assert np.array_equal(out["psi_f"], ref["psi_f"])
+    finally:
+        for s in solvers:
+            s.close()

@@ -19,10 +19,10 @@ from tests._util import rel_err
 pytestmark = pytest.mark.gpu
 
 
-def _problem(seed=5, state_seed=11):
+def _problem(seed=5, state_seed=11, n_tracks_2d=13):
     import simplemoc_gb300 as sm
     spec = sm.ProblemSpec(n_groups=22, fai=5, cai=4, height=200.0, n_sources=300,
-                          n_tracks_2d=13, n_polar=4, z_stacked=10, n_seg=30, seed=seed)
+                          n_tracks_2d=n_tracks_2d, n_polar=4, z_stacked=10, n_seg=30, seed=seed)
     hp = sm.generate(spec)
     rng = np.random.default_rng(state_seed)
     hp.fine_flux[:] = rng.random(hp.fine_flux.size, dtype=np.float32)
@@ -40,10 +40,13 @@ def _other_state(hp):
     return c
 
 
-@pytest.mark.parametrize("mode", ["plain", "mixed"])
-def test_streamed_upload_then_sweep_matches_synchronous(gpu_available, mode):
+@pytest.mark.parametrize("mode,n2d", [("plain", 13), ("mixed", 13), ("plain", 1),
+                                      ("mixed", 300)])
+def test_streamed_upload_then_sweep_matches_synchronous(gpu_available, mode, n2d):
+    """1, 13 and 300 2D tracks: one chunk, three (1, 4, 8 tracks) and five
+    (1, 4, 16, 64, 215 tracks)."""
     import simplemoc_gb300 as sm
-    hp = _problem()
+    hp = _problem(n_tracks_2d=n2d)
     with sm.Solver(hp, mode=mode) as a:
         a.transport_sweep()
         ra = a.download(psi_f=True, fine_flux=True, fine_source=False)
