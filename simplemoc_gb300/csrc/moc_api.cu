@@ -23,6 +23,22 @@ __global__ void widen_kernel(const float *__restrict__ src, double *__restrict__
     dst[i] = (double)src[i];
 }
 
+// phi += phi_in, four floats at a time (n a multiple of 4).
+__global__ void add_kernel(float *__restrict__ phi, const float *__restrict__ phi_in, int64_t n) {
+  float4 *a = reinterpret_cast<float4 *>(phi);
+  const float4 *b = reinterpret_cast<const float4 *>(phi_in);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n / 4;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    float4 x = a[i];
+    const float4 y = b[i];
+    x.x = __fadd_rn(x.x, y.x);
+    x.y = __fadd_rn(x.y, y.y);
+    x.z = __fadd_rn(x.z, y.z);
+    x.w = __fadd_rn(x.w, y.w);
+    a[i] = x;
+  }
+}
+
 __global__ void fold_kernel(float *__restrict__ hi, float *__restrict__ lo, int64_t n) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
@@ -170,7 +186,16 @@ int upload_all(moc_problem *p, const moc_host *h, bool stream_tracks) {
     // the first sweep starts as soon as the first chunk has landed.
     if (!h->fine_source || !h->seg_src) return MOC_ERR_ARG;
     TRY(put_rows(p, p->q, h->fine_source, p->nfsr));
-    TRY(put_rows(p, p->phi, h->fine_flux, p->nfsr));
+    // The scalar flux goes to phi_in on the copy stream, after the chunks, and
+    // phi starts at zero: the first range sweep waits for the fine source only
+    // (1 GB, not 2).  Without room for phi_in it is copied into phi here.
+    if (!p->phi_in && dalloc(p, &p->phi_in, p->nfsr * p->ldg) != MOC_OK) p->phi_in = nullptr;
+    p->phi_fold_pending = false;
+    if (p->phi_in)
+      MOC_CUDA_TRY(cudaMemsetAsync(p->phi, 0, sizeof(float) * (size_t)(p->nfsr * p->ldg),
+                                   p->stream));
+    else
+      TRY(put_rows(p, p->phi, h->fine_flux, p->nfsr));
     TRY(moc_host_validate_except_ids(&d, h));
   }
   Staging sg;
@@ -289,6 +314,10 @@ int upload_all(moc_problem *p, const moc_host *h, bool stream_tracks) {
       MOC_CUDA_TRY(cudaEventRecord(p->chunk_ev[n], p->copy_stream));
       p->chunk_end[n] = i1;
     }
+    if (p->phi_in) {
+      TRY(put_rows(p, p->phi_in, h->fine_flux, p->nfsr, p->copy_stream));
+      p->phi_fold_pending = true;
+    }
     TRY(put_rows(p, p->psi_b, h->psi_b, p->n3d, p->copy_stream));
     MOC_CUDA_TRY(cudaEventRecord(p->copy_done, p->copy_stream));
     p->n_chunks = n;
@@ -317,6 +346,7 @@ void release(moc_problem *p) {
   dfree(p->seg_ds); dfree(p->seg_src); dfree(p->weight); dfree(p->z0); dfree(p->mu);
   dfree(p->src_sigt); dfree(p->src_xs); dfree(p->vol); dfree(p->coef); dfree(p->xs);
   dfree(p->scatter_t); dfree(p->table); dfree(p->q); dfree(p->phi); dfree(p->phi_lo);
+  dfree(p->phi_in);
   dfree(p->psi_f); dfree(p->psi_b); dfree(p->q64); dfree(p->phi64); dfree(p->psi_f64);
   dfree(p->psi_b64); dfree(p->partials); dfree(p->scalars); dfree(p->err);
   dfree(p->xs_order); dfree(p->upd_items); dfree(p->psi_scale); dfree(p->psi_b_nonzero);
@@ -454,6 +484,12 @@ int moc_join_upload(moc_problem *p) {
   if (p->n_chunks == 0) return MOC_OK;
   p->n_chunks = 0;
   MOC_CUDA_TRY(cudaStreamWaitEvent(p->stream, p->copy_done, 0));
+  if (p->phi_fold_pending) {         // the uploaded scalar flux under the tallies
+    p->phi_fold_pending = false;
+    add_kernel<<<1024, 256, 0, p->stream>>>(p->phi, p->phi_in, p->nfsr * p->ldg);
+    MOC_CUDA_TRY(cudaGetLastError());
+    p->launches++;
+  }
   if (p->detect_pending) {
     p->detect_pending = false;
     return moc_detect_psi_b(p);
@@ -626,6 +662,7 @@ int moc_upload(moc_problem *p, const moc_host *host) {
   cudaStreamSynchronize(p->stream);
   p->n_chunks = 0;
   p->detect_pending = false;
+  p->phi_fold_pending = false;
   p->stale = true;
   return rc == MOC_ERR_ARG ? rc : fail(p, rc);
 }

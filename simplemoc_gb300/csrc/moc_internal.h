@@ -122,6 +122,11 @@ struct moc_problem {
   int64_t chunk_end[MAX_UPLOAD_CHUNKS] = {};     // one past the chunk's last 2D track
   int n_chunks = 0;
   bool detect_pending = false;                   // psi_b's nonzero flag still to be set
+  // A streamed upload copies the scalar flux into phi_in on the copy stream
+  // and zeroes phi, so that the first sweep need not wait for it: the sweep
+  // tallies into phi, and the join adds phi_in (the same sum in another order).
+  float *phi_in = nullptr;
+  bool phi_fold_pending = false;
   bool stale = false;                            // rejected input: device state undefined
   void *h_stage = nullptr;                       // pinned host staging of derived arrays
   cudaEvent_t stage_ev = nullptr;                // after the last copy from h_stage
