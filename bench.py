@@ -5,8 +5,9 @@
 
 CONFIG: default (the headline), batched (64 independent cores in one launch,
 CUDA-graph power iteration), adjoint (adjoint / forward sweep time), dropin
-(power iterations through the reference's own entry points), small and
-default_1k (parity and profiling sizes).
+(power iterations through the reference's own entry points), flat (the default
+problem with the flat source, axial_exp = 0), small and default_1k (parity and
+profiling sizes).
 
 A step is one power iteration of src/main.c:57-92 (transport sweep,
 renormalize_flux, update_sources, compute_keff) over the whole problem; the
@@ -52,8 +53,8 @@ def _args():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--config", choices=["default", "small", "default_1k", "batched", "adjoint",
-                                         "dropin"],
+    ap.add_argument("--config", choices=["default", "small", "default_1k", "flat", "batched",
+                                         "adjoint", "dropin"],
                     default="default")
     ap.add_argument("--cores", type=int, default=64, help="cores of the batched workload")
     ap.add_argument("--no-e2e", action="store_true")
@@ -573,7 +574,7 @@ def main():
     peak, peak_kind = _peaks()
     alg_bytes = spec.algorithmic_bytes()
     achieved = alg_bytes / (sweep_ms / 1e3) / 1e9
-    traffic = _traffic_from_profiles()
+    traffic = _traffic_from_profiles() if args.config == "default" else None
     if rank == 0:
         line = {
             "metric": "segment-group integrations/s per sweep, chosen vs plain @ FSR flux rel "

@@ -96,7 +96,12 @@ CONFIG_DEFAULT = ProblemSpec(
 # L2) swept by 1024 of its 16384 2D tracks: the profiling case (~3 GB).
 CONFIG_DEFAULT_1K = CONFIG_DEFAULT.with_(n_tracks_2d=1024)
 
-CONFIGS = {"small": CONFIG_SMALL, "default": CONFIG_DEFAULT, "default_1k": CONFIG_DEFAULT_1K}
+# The default problem with the flat source (axial_exp = 0,
+# attenuate_FSR_fluxes): one fine-source row per segment instead of three.
+CONFIG_DEFAULT_FLAT = CONFIG_DEFAULT.with_(axial_exp=0)
+
+CONFIGS = {"small": CONFIG_SMALL, "default": CONFIG_DEFAULT, "default_1k": CONFIG_DEFAULT_1K,
+           "flat": CONFIG_DEFAULT_FLAT}
 
 
 def exp_table(precision: float, maxval: float = 10.0):
