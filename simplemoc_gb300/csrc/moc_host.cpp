@@ -189,7 +189,7 @@ extern "C" int moc_generate(const moc_dims *d, const moc_gen_params *gp, float *
 int moc_host_derive(const moc_dims *d, const moc_host *h, int32_t ldg, float *seg_ds, float *mu,
                     float *weight, float *coef, float *scatter_t, float *max_abs_dz) {
   const int64_t G = d->n_groups, P = d->n_polar, Z = d->z_stacked, S = d->n_seg;
-  const int64_t N2D = d->n_tracks_2d, N3D = N2D * P * Z;
+  const int64_t N2D = d->n_tracks_2d;
   float worst = 0.0f;
   int nonfinite = 0;
   for (int64_t j = 0; j < P; j++) mu[j] = (float)cos((double)h->polar_angles[j]);   // src/solver.c:373
@@ -209,10 +209,12 @@ int moc_host_derive(const moc_dims *d, const moc_host *h, int32_t ldg, float *se
     }
   }
   *max_abs_dz = nonfinite ? INFINITY : worst;
+  const int64_t PZ = P * Z;
 #pragma omp parallel for schedule(static)
-  for (int64_t t = 0; t < N3D; t++) {
-    const int64_t i = t / (P * Z);
-    weight[t] = h->p_weight[t] * h->az_weight[i];                          // src/solver.c:49
+  for (int64_t i = 0; i < N2D; i++) {
+    const float az = h->az_weight[i];
+    for (int64_t t = i * PZ; t < (i + 1) * PZ; t++)
+      weight[t] = h->p_weight[t] * az;                                     // src/solver.c:49
   }
   moc_host_coef(d, h->sigt, ldg, coef);
   for (int64_t m = 0; m < d->n_xs; m++)

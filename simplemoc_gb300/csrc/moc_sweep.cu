@@ -34,7 +34,6 @@ namespace {
 
 constexpr int MODE_PLAIN = MOC_MODE_PLAIN;
 constexpr int MODE_MIXED = MOC_MODE_MIXED;
-constexpr int MODE_FP64 = MOC_MODE_FP64;
 constexpr int BLOCK = 256;
 constexpr unsigned FULL = 0xffffffffu;
 
