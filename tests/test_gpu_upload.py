@@ -161,3 +161,28 @@ def test_create_rejects_bad_source_ids(gpu_available):
     with pytest.raises(sm.MocError) as e:
         sm.Solver(bad, mode="plain")
     assert e.value.status == MOC_ERR_ARG
+
+
+def test_streamed_upload_without_room_for_the_flux_side_buffer(gpu_available):
+    """A streamed upload copies the scalar flux into a side buffer and adds it
+    after the sweep; when the handle may not allocate that buffer (a capped
+    device budget) the flux is copied into place instead, with the same result."""
+    import simplemoc_gb300 as sm
+    from simplemoc_gb300 import _lib as L
+    hp = _problem(seed=12)
+    with sm.Solver(hp, mode="plain") as a:
+        a.transport_sweep()
+        ra = a.download(psi_f=True, fine_flux=True, fine_source=False)
+    lib = L._lib()
+    with sm.Solver(_other_state(hp), mode="plain") as b:
+        held = int(lib.moc_device_bytes(b.handle))
+        try:
+            L.check(lib.moc_set_memory_limit(held + 4096), "limit")   # no room for 1 flux copy
+            b.upload(hp)
+            b.transport_sweep()
+            rb = b.download(psi_f=True, fine_flux=True, fine_source=False)
+            assert int(lib.moc_device_bytes(b.handle)) == held
+        finally:
+            L.check(lib.moc_set_memory_limit(0), "limit")
+    assert np.array_equal(ra["psi_f"], rb["psi_f"])
+    assert rel_err(rb["fine_flux"], ra["fine_flux"]) <= 1e-5
