@@ -250,6 +250,26 @@ def test_full_small_problem_track_sample_bit_exact(gpu_available, port):
     assert np.abs(out["fine_flux"]).max() > 0
 
 
+@pytest.mark.parametrize("config", ["default", "flat"])
+def test_default_problem_track_sample_bit_exact(gpu_available, port, config):
+    """The default problem at full size (13.1 M tracks, 6.55e10 integrations,
+    2.5 M FSRs), quadratic and flat source: after one PLAIN sweep the angular
+    flux of a random sample of tracks equals the oracle's bit for bit (each
+    track's psi depends only on its own segments and the source storage)."""
+    import simplemoc_gb300 as sm
+    spec = sm.CONFIGS[config]
+    hp = sm.generate(spec)
+    with _solver(hp) as s:
+        s.transport_sweep()
+        out = s.download(psi_f=True, fine_flux=False, fine_source=False)
+    rng = np.random.default_rng(1)
+    tracks = np.sort(rng.choice(spec.n_tracks_3d, 2000, replace=False))
+    psi0 = np.zeros(spec.n_tracks_3d * spec.n_groups, dtype=np.float32)
+    ref = port.sweep_tracks(oracle.make_problem(hp), hp.fine_source, tracks, psi0)
+    got = out["psi_f"].reshape(-1, spec.n_groups)[tracks].ravel()
+    assert np.array_equal(got, ref)
+
+
 def test_full_small_problem_fluxes_vs_parallel_oracle(gpu_available, port):
     """The small problem at full size: every FSR flux after one sweep agrees
     with the oracle's OpenMP sweep of all 1.2 M tracks (normwise 1e-5)."""
