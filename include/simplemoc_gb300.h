@@ -154,7 +154,12 @@ int moc_destroy(moc_problem *p);
  * of range is swept as source 0); the first call after that sweep that waits
  * for the device returns MOC_ERR_ARG.  Either way every other call then
  * returns MOC_ERR_STATE until an upload succeeds (the device state is partly
- * overwritten); the handle itself stays usable for that upload. */
+ * overwritten); the handle itself stays usable for that upload.
+ * The scalar flux of a streamed upload goes to a side buffer (one more
+ * fine_flux-sized array, allocated by the first streamed upload when the
+ * handle's device budget allows, else the flux is copied into place) and is
+ * added to the sweep's tallies once it has landed, so the first sweep waits
+ * for the fine source only. */
 int moc_upload(moc_problem *p, const moc_host *host);
 /* Copies results back (any pointer may be NULL to skip that array). */
 int moc_download(moc_problem *p, float *fine_flux, float *fine_source,
