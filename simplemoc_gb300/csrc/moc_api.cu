@@ -749,10 +749,11 @@ int moc_set_launch(moc_problem *p, int threads_per_track, int chunks_per_thread)
     p->tpw = p->cpl = 0;
     return MOC_OK;
   }
-  static const int ok[][2] = {{32, 1}, {32, 2}, {32, 4}, {16, 1}, {16, 2}, {8, 1}, {8, 4}, {4, 2}};
+  static const int ok[][2] = {{32, 1}, {32, 2}, {32, 4}, {16, 1}, {16, 2}, {8, 1}, {8, 4}, {4, 2},
+                              {10, 5}};
   for (auto &s : ok) {
     if (s[0] == threads_per_track && s[1] == chunks_per_thread) {
-      if ((int64_t)threads_per_track * chunks_per_thread * 4 < p->ldg) return MOC_ERR_ARG;
+      if (moc_shape_groups(threads_per_track, chunks_per_thread) < p->ldg) return MOC_ERR_ARG;
       p->tpw = threads_per_track;
       p->cpl = chunks_per_thread;
       return MOC_OK;

@@ -144,6 +144,10 @@ constexpr int32_t MOC_DEV_ERR_ARG = 1;        // an argument error found by a ke
 constexpr int32_t MOC_DEV_ERR_TIMEOUT = 2;    // a bounded device wait gave up
 constexpr int32_t MOC_DEV_ERR_SOURCE = 4;     // a segment source id out of range
 
+// Groups one track covers with a launch shape: TPW x CPL chunks of 4 groups,
+// or of 2 groups when TPW is not a power of two (10 x 5: 100 groups).
+int moc_shape_groups(int tpw, int cpl);
+
 // Launchers implemented in moc_sweep.cu / moc_post.cu.
 int moc_launch_sweep(moc_problem *p);
 // The sweep of 2D tracks [i2_begin, i2_end) with all their 3D tracks.

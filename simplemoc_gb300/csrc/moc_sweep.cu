@@ -76,6 +76,19 @@ __device__ __forceinline__ void red_add_v4_last(float *p, float4 t, uint64_t pol
   asm volatile("red.global.add.L2::cache_hint.v4.f32 [%0], {%1,%2,%3,%4}, %5;" ::"l"(p),
                "f"(t.x), "f"(t.y), "f"(t.z), "f"(t.w), "l"(pol));
 }
+__device__ __forceinline__ void red_add_vec_last(float *p, float4 t, uint64_t pol) {
+  red_add_v4_last(p, t, pol);
+}
+__device__ __forceinline__ void red_add_vec_last(float *p, float2 t, uint64_t pol) {
+  asm volatile("red.global.add.L2::cache_hint.v2.f32 [%0], {%1,%2}, %3;" ::"l"(p), "f"(t.x),
+               "f"(t.y), "l"(pol));
+}
+__device__ __forceinline__ void red_add_vec(float *p, float4 t) {
+  red_add_v4(p, t.x, t.y, t.z, t.w);
+}
+__device__ __forceinline__ void red_add_vec(float *p, float2 t) {
+  asm volatile("red.global.add.v2.f32 [%0], {%1,%2};" ::"l"(p), "f"(t.x), "f"(t.y));
+}
 
 __device__ __forceinline__ float get(const float4 &v, int e) {
   return e == 0 ? v.x : e == 1 ? v.y : e == 2 ? v.z : v.w;
@@ -85,6 +98,39 @@ __device__ __forceinline__ void set(float4 &v, int e, float x) {
   else if (e == 1) v.y = x;
   else if (e == 2) v.z = x;
   else v.w = x;
+}
+__device__ __forceinline__ float get(const float2 &v, int e) { return e == 0 ? v.x : v.y; }
+__device__ __forceinline__ void set(float2 &v, int e, float x) {
+  if (e == 0) v.x = x;
+  else v.y = x;
+}
+
+// A chunk of the group axis: VW = 4 consecutive groups (float4) or 2 (float2).
+// Two-group chunks let a track of G groups fill lane counts that are not a
+// power of two (100 groups: 10 lanes x 5 chunks, three tracks a warp).
+template <int VW>
+struct VecOf;
+template <>
+struct VecOf<4> {
+  using T = float4;
+};
+template <>
+struct VecOf<2> {
+  using T = float2;
+};
+
+__device__ __forceinline__ void vzero(float4 &v) { v = make_float4(0.f, 0.f, 0.f, 0.f); }
+__device__ __forceinline__ void vzero(float2 &v) { v = make_float2(0.f, 0.f); }
+
+__device__ __forceinline__ void ld_stream_vec(const float *p, float4 &v) { v = ld_stream(p); }
+__device__ __forceinline__ void ld_stream_vec(const float *p, float2 &v) {
+  asm("ld.global.nc.L1::no_allocate.v2.f32 {%0,%1}, [%2];" : "=f"(v.x), "=f"(v.y) : "l"(p));
+}
+__device__ __forceinline__ void ldg_vec(const float *p, float4 &v) {
+  v = __ldg(reinterpret_cast<const float4 *>(p));
+}
+__device__ __forceinline__ void ldg_vec(const float *p, float2 &v) {
+  v = __ldg(reinterpret_cast<const float2 *>(p));
 }
 
 // Reference interpolation table, src/solver.c:1441-1464.
@@ -272,23 +318,24 @@ __device__ __forceinline__ void comp_add(float *hi, float *lo, float x) {
 
 // Loads of one segment that are issued one segment ahead (software pipeline):
 // the three fine-source rows (one row for the flat source) of every chunk.
-template <int CPL, bool QUAD>
+template <int CPL, bool QUAD, int VW = 4>
 struct Rows {
-  float4 v[CPL][QUAD ? 3 : 1];
+  typename VecOf<VW>::T v[CPL][QUAD ? 3 : 1];
 };
 
-template <int CPL, bool QUAD>
+// nch = chunks of VW groups in a row (ldg / VW).
+template <int CPL, bool QUAD, int VW = 4>
 __device__ __forceinline__ void load_rows(const SweepArgs &a, const Seg &g, int li, int TPW,
-                                          Rows<CPL, QUAD> &r) {
+                                          Rows<CPL, QUAD, VW> &r, int nch) {
 #pragma unroll
   for (int k = 0; k < CPL; ++k) {
     const int c = li + TPW * k;
-    if (c < a.nchunk) {
-      const float *qr = a.q + g.qrow + 4 * c;
-      r.v[k][0] = ld_stream(qr);
+    if (c < nch) {
+      const float *qr = a.q + g.qrow + VW * c;
+      ld_stream_vec(qr, r.v[k][0]);
       if (QUAD) {
-        r.v[k][QUAD ? 1 : 0] = ld_stream(qr + a.ldg);
-        r.v[k][QUAD ? 2 : 0] = ld_stream(qr + 2 * a.ldg);
+        ld_stream_vec(qr + a.ldg, r.v[k][QUAD ? 1 : 0]);
+        ld_stream_vec(qr + 2 * a.ldg, r.v[k][QUAD ? 2 : 0]);
       }
     }
   }
@@ -311,11 +358,20 @@ __device__ __forceinline__ int checked_source(const SweepArgs &a, int s, int li)
 // One 3D track (or one group of TPW lanes' track) of the sweep.  TPW_CT is
 // the threads per track when known at compile time; 0 takes tpw_rt (the
 // batched kernel, where each core has its own width).
-template <int TPW_CT, int CPL, int MODE, bool QUAD, bool CSR, bool CKPT = false>
+template <int TPW_CT, int CPL, int MODE, bool QUAD, bool CSR, bool CKPT = false, int VW = 4>
 __device__ __forceinline__ void sweep_track(const SweepArgs &a, int64_t track, int lane,
                                             int tpw_rt, const float2 *s_table) {
   const int TPW = TPW_CT ? TPW_CT : tpw_rt;
   const int li = lane % TPW;
+  const int gb = lane - li;              // the track's first lane
+  // lane k of the track: a width-TPW shuffle for power-of-two widths, the
+  // absolute lane gb + k otherwise
+  constexpr bool POW2 = TPW_CT > 0 && (TPW_CT & (TPW_CT - 1)) == 0;
+  auto tshfl = [&](auto v, int k) {
+    return (POW2 || TPW_CT == 0) ? __shfl_sync(FULL, v, k, TPW) : __shfl_sync(FULL, v, gb + k);
+  };
+  using V = typename VecOf<VW>::T;
+  const int nch = VW == 4 ? a.nchunk : a.ldg / VW;   // chunks of VW groups in a row
   const int64_t PZ = (int64_t)a.P * a.Z;
   const bool valid = track < a.n3d;
   const int64_t tr = valid ? track : a.n3d - 1;
@@ -344,18 +400,16 @@ __device__ __forceinline__ void sweep_track(const SweepArgs &a, int64_t track, i
     srcb = a.seg_src + tr * S;
   }
 
-  float4 psi[CPL];
+  V psi[CPL];
 #pragma unroll
   for (int k = 0; k < CPL; ++k) {
     const int c = li + TPW * k;
-    psi[k] = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (c < a.nchunk) psi[k] = *reinterpret_cast<const float4 *>(a.psi + tr * a.ldg + 4 * c);
+    vzero(psi[k]);
+    if (c < nch) psi[k] = *reinterpret_cast<const V *>(a.psi + tr * a.ldg + VW * c);
     if (a.psi_scale) {                    // renormalisation still to apply (src/solver.c:1224)
       const float sc = *a.psi_scale;
-      psi[k].x = __fmul_rn(psi[k].x, sc);
-      psi[k].y = __fmul_rn(psi[k].y, sc);
-      psi[k].z = __fmul_rn(psi[k].z, sc);
-      psi[k].w = __fmul_rn(psi[k].w, sc);
+#pragma unroll
+      for (int e = 0; e < VW; ++e) set(psi[k], e, __fmul_rn(get(psi[k], e), sc));
     }
   }
 
@@ -368,16 +422,16 @@ __device__ __forceinline__ void sweep_track(const SweepArgs &a, int64_t track, i
   if (CSR) {
     z_c = li < S ? __ldg(zb + li) : 0.f;
     z_n = TPW + li < S ? __ldg(zb + TPW + li) : 0.f;
-    z = __shfl_sync(FULL, z_c, 0, TPW);
+    z = tshfl(z_c, 0);
   }
 
-  float ds = __shfl_sync(FULL, ds_c, 0, TPW);
-  Seg g = segment_geometry(a, z, checked_source(a, __shfl_sync(FULL, src_c, 0, TPW), li));
+  float ds = tshfl(ds_c, 0);
+  Seg g = segment_geometry(a, z, checked_source(a, tshfl(src_c, 0), li));
   int S_loop = S;                        // the warp's longest track (CSR, several a warp)
   if (CSR && TPW < 32) S_loop = (int)__reduce_max_sync(FULL, (unsigned)S);
   const uint64_t tally_pol = MODE == MODE_MIXED ? l2_evict_last_policy() : 0;
-  Rows<CPL, QUAD> rows;
-  if (S_loop > 0) load_rows<CPL, QUAD>(a, g, li, TPW, rows);
+  Rows<CPL, QUAD, VW> rows;
+  if (S_loop > 0) load_rows<CPL, QUAD, VW>(a, g, li, TPW, rows, nch);
 
   int ck_left = 0;                       // segments to the next checkpoint
   int64_t ck_slot = CKPT ? tr * a.ck_n : 0;
@@ -391,8 +445,7 @@ __device__ __forceinline__ void sweep_track(const SweepArgs &a, int64_t track, i
 #pragma unroll
         for (int k = 0; k < CPL; ++k) {
           const int c = li + TPW * k;
-          if (c < a.nchunk)
-            *reinterpret_cast<float4 *>(a.ck_psi + ck_slot * a.ldg + 4 * c) = psi[k];
+          if (c < nch) *reinterpret_cast<V *>(a.ck_psi + ck_slot * a.ldg + VW * c) = psi[k];
         }
         if (li == 0) a.ck_z[ck_slot] = z;
       }
@@ -402,10 +455,10 @@ __device__ __forceinline__ void sweep_track(const SweepArgs &a, int64_t track, i
     // ---- issue the loads of segment n+1 before the arithmetic of segment n
     float ds1 = 0.f;
     Seg g1 = g;
-    Rows<CPL, QUAD> rows1 = rows;
+    Rows<CPL, QUAD, VW> rows1 = rows;
     const int m = n + 1;
     if (m < S_loop) {
-      const int k = m & (TPW - 1);
+      const int k = (POW2 || TPW_CT == 0) ? (m & (TPW - 1)) : m % TPW;
       if (k == 0) {
         ds_c = ds_n;
         src_c = src_n;
@@ -417,32 +470,36 @@ __device__ __forceinline__ void sweep_track(const SweepArgs &a, int64_t track, i
           z_n = nl < S ? __ldg(zb + nl) : 0.f;
         }
       }
-      if (CSR) z_next = __shfl_sync(FULL, z_c, k, TPW);
-      ds1 = __shfl_sync(FULL, ds_c, k, TPW);
-      g1 = segment_geometry(a, z_next, checked_source(a, __shfl_sync(FULL, src_c, k, TPW), li));
-      load_rows<CPL, QUAD>(a, g1, li, TPW, rows1);
+      if (CSR) z_next = tshfl(z_c, k);
+      ds1 = tshfl(ds_c, k);
+      g1 = segment_geometry(a, z_next, checked_source(a, tshfl(src_c, k), li));
+      load_rows<CPL, QUAD, VW>(a, g1, li, TPW, rows1, nch);
     }
     // ---- segment n
     const MixedFit fit = (MODE == MODE_MIXED && QUAD) ? mixed_fit(a, g.zin, mu, mu2) : MixedFit{};
 #pragma unroll
     for (int k = 0; k < CPL; ++k) {
       const int c = li + TPW * k;
-      if (c >= a.nchunk || !live) continue;
-      const int g4 = 4 * c;
-      const float *cf = a.coef + g.crow + 4 * COEF_PLANES * c;    // this chunk's planes
-      const float4 sig = __ldg(reinterpret_cast<const float4 *>(cf));
-      const float4 r1 = __ldg(reinterpret_cast<const float4 *>(cf + 4));
-      float4 t;
+      if (c >= nch || !live) continue;
+      const int g4 = VW * c;                                      // first group of the chunk
+      // this chunk's planes: the 4-group block holding it, offset within the block
+      const float *cf = VW == 4 ? a.coef + g.crow + 4 * COEF_PLANES * c
+                                : a.coef + g.crow + 4 * COEF_PLANES * (c >> 1) + 2 * (c & 1);
+      V sig, r1;
+      ldg_vec(cf, sig);
+      ldg_vec(cf + 4, r1);
+      V t;
       if (QUAD) {
-        const float4 y1 = rows.v[k][0];
-        const float4 y2 = rows.v[k][QUAD ? 1 : 0];
-        const float4 y3 = rows.v[k][QUAD ? 2 : 0];
+        const V y1 = rows.v[k][0];
+        const V y2 = rows.v[k][QUAD ? 1 : 0];
+        const V y3 = rows.v[k][QUAD ? 2 : 0];
         if (MODE == MODE_PLAIN) {
-          const float4 r2 = __ldg(reinterpret_cast<const float4 *>(cf + 8));
-          const float4 r3 = __ldg(reinterpret_cast<const float4 *>(cf + 12));
-          const float4 r4 = __ldg(reinterpret_cast<const float4 *>(cf + 16));
+          V r2, r3, r4;
+          ldg_vec(cf + 8, r2);
+          ldg_vec(cf + 12, r3);
+          ldg_vec(cf + 16, r4);
 #pragma unroll
-          for (int e = 0; e < 4; ++e) {
+          for (int e = 0; e < VW; ++e) {
             // the reference's divisors, formed with its own operations
             const float sg = get(sig, e);
             const float sg2 = __fmul_rn(sg, sg);                        // solver.c:153
@@ -455,11 +512,12 @@ __device__ __forceinline__ void sweep_track(const SweepArgs &a, int64_t track, i
             set(psi[k], e, p);
           }
         } else {
-          const float4 r2 = __ldg(reinterpret_cast<const float4 *>(cf + 8));
-          const float4 r4 = __ldg(reinterpret_cast<const float4 *>(cf + 16));
-          const float4 r3x2 = __ldg(reinterpret_cast<const float4 *>(cf + 20));
+          V r2, r4, r3x2;
+          ldg_vec(cf + 8, r2);
+          ldg_vec(cf + 16, r4);
+          ldg_vec(cf + 20, r3x2);
 #pragma unroll
-          for (int e = 0; e < 4; ++e) {
+          for (int e = 0; e < VW; ++e) {
             float p = get(psi[k], e);
             set(t, e, mixed_quad(get(y1, e), get(y2, e), get(y3, e), fit, get(sig, e), get(r1, e),
                                  get(r2, e), get(r3x2, e), get(r4, e), ds, w, p));
@@ -467,9 +525,9 @@ __device__ __forceinline__ void sweep_track(const SweepArgs &a, int64_t track, i
           }
         }
       } else {
-        const float4 y = rows.v[k][0];
+        const V y = rows.v[k][0];
 #pragma unroll
-        for (int e = 0; e < 4; ++e) {
+        for (int e = 0; e < VW; ++e) {
           float p = get(psi[k], e);
           if (MODE == MODE_PLAIN)
             set(t, e, plain_flat(a, s_table, get(y, e), get(sig, e), get(r1, e), ds, w_mu, p));
@@ -482,14 +540,12 @@ __device__ __forceinline__ void sweep_track(const SweepArgs &a, int64_t track, i
         float *dst = a.phi + g.frow + g4;
         if (MODE == MODE_MIXED && a.phi_lo != nullptr) {
           float *lo = a.phi_lo + g.frow + g4;
-          comp_add(dst + 0, lo + 0, t.x);
-          comp_add(dst + 1, lo + 1, t.y);
-          comp_add(dst + 2, lo + 2, t.z);
-          comp_add(dst + 3, lo + 3, t.w);
+#pragma unroll
+          for (int e = 0; e < VW; ++e) comp_add(dst + e, lo + e, get(t, e));
         } else if (MODE == MODE_MIXED) {
-          red_add_v4_last(dst, t, tally_pol);
+          red_add_vec_last(dst, t, tally_pol);
         } else {
-          red_add_v4(dst, t.x, t.y, t.z, t.w);
+          red_add_vec(dst, t);
         }
       }
     }
@@ -502,14 +558,16 @@ __device__ __forceinline__ void sweep_track(const SweepArgs &a, int64_t track, i
 #pragma unroll
     for (int k = 0; k < CPL; ++k) {
       const int c = li + TPW * k;
-      if (c < a.nchunk) *reinterpret_cast<float4 *>(a.psi + tr * a.ldg + 4 * c) = psi[k];
+      if (c < nch) *reinterpret_cast<V *>(a.psi + tr * a.ldg + VW * c) = psi[k];
     }
   }
 }
 
-template <int TPW, int CPL, int MODE, bool QUAD, bool CSR = false, bool CKPT = false>
-__global__ void __launch_bounds__(BLOCK) sweep_kernel(SweepArgs a) {
-  extern __shared__ float2 s_table[];
+// With TPW not dividing 32 the last 32 % TPW lanes own no track: they run the
+// loop on an out-of-range track (loads clamped to a real one, no stores) so that
+// the warp's shuffles stay converged.
+template <int TPW, int CPL, int MODE, bool QUAD, bool CSR, bool CKPT, int VW>
+__device__ __forceinline__ void sweep_body(const SweepArgs &a, float2 *s_table) {
   if (MODE == MODE_PLAIN) {
     for (int i = threadIdx.x; i < a.table_n; i += BLOCK) s_table[i] = a.table[i];
     __syncthreads();
@@ -520,7 +578,22 @@ __global__ void __launch_bounds__(BLOCK) sweep_kernel(SweepArgs a) {
   const int64_t warp_id = ((int64_t)blockIdx.x * BLOCK + threadIdx.x) >> 5;
   const int64_t n_warps = ((int64_t)gridDim.x * BLOCK) >> 5;
   for (int64_t base = warp_id * GPW; base < a.n3d; base += n_warps * GPW)
-    sweep_track<TPW, CPL, MODE, QUAD, CSR, CKPT>(a, base + gw, lane, TPW, s_table);
+    sweep_track<TPW, CPL, MODE, QUAD, CSR, CKPT, VW>(a, gw < GPW ? base + gw : a.n3d, lane,
+                                                     TPW, s_table);
+}
+
+template <int TPW, int CPL, int MODE, bool QUAD, bool CSR = false, bool CKPT = false>
+__global__ void __launch_bounds__(BLOCK) sweep_kernel(SweepArgs a) {
+  extern __shared__ float2 s_table[];
+  sweep_body<TPW, CPL, MODE, QUAD, CSR, CKPT, 4>(a, s_table);
+}
+
+// Two-group chunks: held to two blocks an SM (the MIXED quadratic variant
+// would otherwise take 139 registers and run one).
+template <int TPW, int CPL, int MODE, bool QUAD, bool CSR = false, bool CKPT = false>
+__global__ void __launch_bounds__(BLOCK, 2) sweep_kernel_v2(SweepArgs a) {
+  extern __shared__ float2 s_table[];
+  sweep_body<TPW, CPL, MODE, QUAD, CSR, CKPT, 2>(a, s_table);
 }
 
 // ---- Staged sweep.  The fine-source rows of each segment (the three fit rows
@@ -912,9 +985,14 @@ __global__ void __launch_bounds__(BLOCK) sweep64_kernel(SweepArgs a) {
   }
 }
 
-template <int TPW, int CPL, int MODE, bool QUAD, bool CSR = false, bool CKPT = false>
+template <int TPW, int CPL, int MODE, bool QUAD, bool CSR = false, bool CKPT = false,
+          int VW = 4>
 int launch_t(moc_problem *p, const SweepArgs &a) {
-  auto kern = sweep_kernel<TPW, CPL, MODE, QUAD, CSR, CKPT>;
+  void (*kern)(SweepArgs);
+  if constexpr (VW == 4)
+    kern = sweep_kernel<TPW, CPL, MODE, QUAD, CSR, CKPT>;
+  else
+    kern = sweep_kernel_v2<TPW, CPL, MODE, QUAD, CSR, CKPT>;
   size_t smem = (MODE == MODE_PLAIN) ? sizeof(float2) * (size_t)a.table_n : 0;
   if (smem > 48 * 1024) {
     if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
@@ -963,6 +1041,7 @@ int dispatch_shape(moc_problem *p, const SweepArgs &a, int tpw, int cpl) {
   if (tpw == 8 && cpl == 1) return launch_t<8, 1, MODE, QUAD>(p, a);
   if (tpw == 8 && cpl == 4) return launch_t<8, 4, MODE, QUAD>(p, a);
   if (tpw == 4 && cpl == 2) return launch_t<4, 2, MODE, QUAD>(p, a);
+  if (tpw == 10 && cpl == 5) return launch_t<10, 5, MODE, QUAD, false, false, 2>(p, a);
   return MOC_ERR_UNSUPPORTED;
 }
 
@@ -1013,12 +1092,16 @@ int dispatch_staged(moc_problem *p, const SweepArgs &a, int tpw, int cpl, int st
 // Default threads-per-track and chunks-per-thread for a group count, from the
 // launch-shape measurements on GB300 (two tracks per warp with two chunks per
 // thread was fastest for 100 groups in both modes); moc_autotune measures.
+int moc_shape_groups(int tpw, int cpl) {
+  return tpw * cpl * ((tpw & (tpw - 1)) == 0 ? 4 : 2);
+}
+
 int moc_sweep_launch_shape(const moc_problem *p, int *tpw, int *cpl) {
   const int nchunk = p->ldg / 4;
   if (p->tpw > 0) {
     *tpw = p->tpw;
     *cpl = p->cpl;
-    if ((int64_t)p->tpw * p->cpl < nchunk) return MOC_ERR_ARG;
+    if (moc_shape_groups(p->tpw, p->cpl) < p->ldg) return MOC_ERR_ARG;
     return MOC_OK;
   }
   if (nchunk <= 8) { *tpw = 8; *cpl = 1; }
@@ -1191,15 +1274,15 @@ int moc_sweep_autotune(moc_problem *p, int64_t n_sub, int *tpw_out, int *cpl_out
     rc = MOC_ERR_CUDA;
   // register-prefetch shapes, then the staged kernel (4-stage ring) shapes
   static const int shapes[][3] = {{32, 1, 0}, {32, 2, 0}, {32, 4, 0}, {16, 1, 0}, {16, 2, 0},
-                                  {8, 1, 0},  {8, 4, 0},  {4, 2, 0},  {32, 1, 4}, {32, 2, 4},
-                                  {16, 1, 4}, {16, 2, 4}, {8, 1, 4}};
-  const int nchunk = p->ldg / 4;
+                                  {8, 1, 0},  {8, 4, 0},  {4, 2, 0},  {10, 5, 0}, {32, 1, 4},
+                                  {32, 2, 4}, {16, 1, 4}, {16, 2, 4}, {8, 1, 4}};
   double best = 1e30;
   int bt = 0, bc = 0, bs = 0;
   for (auto &sh : shapes) {
     if (rc != MOC_OK) break;
-    if ((int64_t)sh[0] * sh[1] < nchunk) continue;
-    if ((int64_t)sh[0] * sh[1] >= 4 * (int64_t)nchunk && sh[1] > 1) continue;   // mostly idle lanes
+    const int covered = moc_shape_groups(sh[0], sh[1]);
+    if (covered < p->ldg) continue;
+    if (covered >= 4 * p->ldg && sh[1] > 1) continue;                  // mostly idle lanes
     if (sh[2] > 0 && staged_smem(a, p->mode == MOC_MODE_PLAIN ? MODE_PLAIN : MODE_MIXED,
                                  p->d.axial_exp == 2, sh[0], sh[2]) > 227 * 1024)
       continue;
@@ -1347,11 +1430,13 @@ __device__ __forceinline__ AdjOut adj_quad(const SweepArgs &a, float y1, float y
   const float R = fmaf(tau, tau - 2.f, 2.f * e * r3); // the reference's reuse term
   const float Cc = fmaf(tau, fmaf(tau, tau - 3.f, 6.f), -6.f * e);
   const float tme = tau - e;
+  // factors shared by the partials below
+  const float er1 = e * r1, epsds = eps * ds, tmer2 = tme * r2, cr4 = Cc * r4;
   AdjOut o;
-  o.pbar = pbar * eps + abar * e * r1;
-  const float q0b = abar * tme * r2 + pbar * e * r1;
-  const float q1b = mu * (abar * R + pbar * tme * r2);
-  const float q2b = mu2 * (abar * Cc * r4 + pbar * R);
+  o.pbar = fmaf(pbar, eps, abar * er1);
+  const float q0b = fmaf(abar, tmer2, pbar * er1);
+  const float q1b = mu * fmaf(abar, R, pbar * tmer2);
+  const float q2b = mu2 * fmaf(abar, cr4, pbar * R);
   const float c1b = fmaf(q0b, zin, q1b);
   const float c2b = fmaf(fmaf(q0b, zin, 2.f * q1b), zin, q2b);
   o.y1b = c1b * a.rd1 + c2b * a.rd2;
@@ -1360,14 +1445,18 @@ __device__ __forceinline__ AdjOut adj_quad(const SweepArgs &a, float y1, float y
   o.c0b = q0b;                                        // q0 = c0 + c1 zin + c2 zin^2
   o.c1b = c1b;
   o.c2b = c2b;
-  const float A = (q0 * tau + (sig * psi - q0) * e) * r2;
-  const float dA = (q0 * ds + psi * e + (sig * psi - q0) * eps * ds) * r2 - 2.f * A * r1;
-  const float dR = (2.f * tau - 2.f) * ds + 2.f * eps * ds * r3 - 6.f * e * r3 * r1;
-  const float dC = ((3.f * tau - 6.f) * tau + 6.f) * ds - 6.f * eps * ds;
-  const float dfi = dA + q1 * mu * dR + q2 * mu2 * (dC * r4 - 4.f * Cc * r4 * r1);
-  const float dpn = q0 * (eps * ds * r1 - e * r2) + q1 * mu * (e * ds * r2 - 2.f * tme * r3) +
-                    q2 * mu2 * dR - psi * eps * ds;
-  o.sbar = abar * dfi + pbar * dpn;
+  // d/dsigma of the flux integral (A + q1 mu R + q2 mu^2 C/(3 sig^4)) and of the
+  // outgoing psi, with dtau/dsigma = ds and dE/dsigma = eps ds
+  const float sp = sig * psi - q0;
+  const float A = fmaf(q0, tau, sp * e) * r2;
+  const float dA = fmaf(fmaf(q0, ds, fmaf(psi, e, sp * epsds)), r2, -2.f * A * r1);
+  const float dR = fmaf(2.f * tau - 2.f, ds, r3 * fmaf(2.f, epsds, -6.f * er1));
+  const float dC = fmaf(fmaf(3.f * tau - 6.f, tau, 6.f), ds, -6.f * epsds);
+  const float q1mu = q1 * mu, q2mu2 = q2 * mu2;
+  const float dfi = fmaf(q1mu, dR, fmaf(q2mu2, fmaf(dC, r4, -4.f * cr4 * r1), dA));
+  const float dpn = fmaf(q0 * r1, epsds - er1,
+                         fmaf(q1mu, fmaf(e * ds, r2, -2.f * tme * r3), fmaf(q2mu2, dR, -psi * epsds)));
+  o.sbar = fmaf(abar, dfi, pbar * dpn);
   return o;
 }
 
@@ -1666,6 +1755,9 @@ template <bool QUAD>
 int dispatch_ckpt(moc_problem *p, const SweepArgs &a) {
   const int nchunk = p->ldg / 4;
   if (nchunk <= 8) return launch_t<8, 1, MODE_MIXED, QUAD, false, true>(p, a);
+  // 33 to 100 groups: two-group chunks, three tracks a warp (the forward sweep's
+  // 10 x 5 shape; 16 lanes of float4 chunks would leave most of them idle)
+  if (p->ldg <= 100) return launch_t<10, 5, MODE_MIXED, QUAD, false, true, 2>(p, a);
   if (nchunk <= 16) return launch_t<16, 1, MODE_MIXED, QUAD, false, true>(p, a);
   if (nchunk <= 32) return launch_t<32, 1, MODE_MIXED, QUAD, false, true>(p, a);
   if (nchunk <= 64) return launch_t<32, 2, MODE_MIXED, QUAD, false, true>(p, a);
