@@ -122,9 +122,28 @@ struct VecOf<2> {
 __device__ __forceinline__ void vzero(float4 &v) { v = make_float4(0.f, 0.f, 0.f, 0.f); }
 __device__ __forceinline__ void vzero(float2 &v) { v = make_float2(0.f, 0.f); }
 
-__device__ __forceinline__ void ld_stream_vec(const float *p, float4 &v) { v = ld_stream(p); }
-__device__ __forceinline__ void ld_stream_vec(const float *p, float2 &v) {
-  asm("ld.global.nc.L1::no_allocate.v2.f32 {%0,%1}, [%2];" : "=f"(v.x), "=f"(v.y) : "l"(p));
+// Fine-source row loads.  L1A: allocate in L1, so that the loads of one row by
+// several instructions (a row is 400 bytes at 100 groups, split across lanes
+// and chunks at boundaries that need not fall on a 32-byte sector) meet in L1
+// instead of each fetching the shared sectors.  Measured on the default
+// problem: MIXED 234.6 -> 227.1 ms at 16 x 2 and 254 -> 226.7 ms at 10 x 5,
+// PLAIN 311.5 -> 303.5 ms at 10 x 5; PLAIN at 16 x 2 was 1 % slower with it
+// and goes without.
+template <bool L1A>
+__device__ __forceinline__ void ld_row_vec(const float *p, float4 &v) {
+  if (L1A)
+    asm("ld.global.nc.v4.f32 {%0,%1,%2,%3}, [%4];"
+        : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+        : "l"(p));
+  else
+    v = ld_stream(p);
+}
+template <bool L1A>
+__device__ __forceinline__ void ld_row_vec(const float *p, float2 &v) {
+  if (L1A)
+    asm("ld.global.nc.v2.f32 {%0,%1}, [%2];" : "=f"(v.x), "=f"(v.y) : "l"(p));
+  else
+    asm("ld.global.nc.L1::no_allocate.v2.f32 {%0,%1}, [%2];" : "=f"(v.x), "=f"(v.y) : "l"(p));
 }
 __device__ __forceinline__ void ldg_vec(const float *p, float4 &v) {
   v = __ldg(reinterpret_cast<const float4 *>(p));
@@ -324,7 +343,7 @@ struct Rows {
 };
 
 // nch = chunks of VW groups in a row (ldg / VW).
-template <int CPL, bool QUAD, int VW = 4>
+template <int CPL, bool QUAD, int VW, bool L1A>
 __device__ __forceinline__ void load_rows(const SweepArgs &a, const Seg &g, int li, int TPW,
                                           Rows<CPL, QUAD, VW> &r, int nch) {
 #pragma unroll
@@ -332,10 +351,10 @@ __device__ __forceinline__ void load_rows(const SweepArgs &a, const Seg &g, int 
     const int c = li + TPW * k;
     if (c < nch) {
       const float *qr = a.q + g.qrow + VW * c;
-      ld_stream_vec(qr, r.v[k][0]);
+      ld_row_vec<L1A>(qr, r.v[k][0]);
       if (QUAD) {
-        ld_stream_vec(qr + a.ldg, r.v[k][QUAD ? 1 : 0]);
-        ld_stream_vec(qr + 2 * a.ldg, r.v[k][QUAD ? 2 : 0]);
+        ld_row_vec<L1A>(qr + a.ldg, r.v[k][QUAD ? 1 : 0]);
+        ld_row_vec<L1A>(qr + 2 * a.ldg, r.v[k][QUAD ? 2 : 0]);
       }
     }
   }
@@ -371,6 +390,7 @@ __device__ __forceinline__ void sweep_track(const SweepArgs &a, int64_t track, i
     return (POW2 || TPW_CT == 0) ? __shfl_sync(FULL, v, k, TPW) : __shfl_sync(FULL, v, gb + k);
   };
   using V = typename VecOf<VW>::T;
+  constexpr bool L1A = MODE == MODE_MIXED || VW == 2;   // row loads allocate in L1
   const int nch = VW == 4 ? a.nchunk : a.ldg / VW;   // chunks of VW groups in a row
   const int64_t PZ = (int64_t)a.P * a.Z;
   const bool valid = track < a.n3d;
@@ -431,7 +451,7 @@ __device__ __forceinline__ void sweep_track(const SweepArgs &a, int64_t track, i
   if (CSR && TPW < 32) S_loop = (int)__reduce_max_sync(FULL, (unsigned)S);
   const uint64_t tally_pol = MODE == MODE_MIXED ? l2_evict_last_policy() : 0;
   Rows<CPL, QUAD, VW> rows;
-  if (S_loop > 0) load_rows<CPL, QUAD, VW>(a, g, li, TPW, rows, nch);
+  if (S_loop > 0) load_rows<CPL, QUAD, VW, L1A>(a, g, li, TPW, rows, nch);
 
   int ck_left = 0;                       // segments to the next checkpoint
   int64_t ck_slot = CKPT ? tr * a.ck_n : 0;
@@ -473,7 +493,7 @@ __device__ __forceinline__ void sweep_track(const SweepArgs &a, int64_t track, i
       if (CSR) z_next = tshfl(z_c, k);
       ds1 = tshfl(ds_c, k);
       g1 = segment_geometry(a, z_next, checked_source(a, tshfl(src_c, k), li));
-      load_rows<CPL, QUAD, VW>(a, g1, li, TPW, rows1, nch);
+      load_rows<CPL, QUAD, VW, L1A>(a, g1, li, TPW, rows1, nch);
     }
     // ---- segment n
     const MixedFit fit = (MODE == MODE_MIXED && QUAD) ? mixed_fit(a, g.zin, mu, mu2) : MixedFit{};
