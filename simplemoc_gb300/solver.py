@@ -98,8 +98,12 @@ class Solver:
     def upload(self, problem: HostProblem | None = None) -> None:
         """Copies `problem` (default: the problem the solver was made with) to
         the device.  The per-track copies may still be in flight when this
-        returns; the arrays are kept referenced until the next upload."""
+        returns.  The arrays of this upload and of the one before it stay
+        referenced: an upload joins the copies of the one before on the device
+        only, and its own staging wait is what retires the copies of the upload
+        two back."""
         p = problem or self.problem
+        self._host_prev = getattr(self, "_host_problem", None)
         self._host = p.host()
         self._host_problem = p
         L.check(self._lib.moc_upload(self._h, C.byref(self._host)), "moc_upload")
