@@ -329,7 +329,11 @@ int moc_batch_sweep(moc_batch *b);
 /* `iters` power iterations of every core (batched sweep, then each core's
  * renormalize_flux / update_sources / compute_keff with k_eff kept on the
  * device); use_graph captures one iteration as a CUDA graph and replays it.
- * *ms_total = device time of the iterations (events on the batch stream). */
+ * Before it captures (its first call, and the first after an upload or a mode
+ * flag change of a core) it runs one iteration without the graph, so that call
+ * makes iters + 1 iterations.  *ms_total = device time of the `iters`
+ * iterations (events on the batch stream).  Each call first waits for the
+ * cores' own streams and refreshes their sweep arguments. */
 int moc_batch_power_iterations(moc_batch *b, int iters, int use_graph,
                                double *ms_total);
 /* Per-core k_eff and source residual of the last iteration. */

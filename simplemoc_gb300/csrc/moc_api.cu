@@ -651,6 +651,7 @@ int moc_upload(moc_problem *p, const moc_host *host) {
     rc = moc_host_validate(&p->d, host);
     if (rc != MOC_OK) return rc;
   }
+  p->uploads++;
   rc = upload_all(p, host, streamed);
   if (rc == MOC_OK) {
     p->stale = false;

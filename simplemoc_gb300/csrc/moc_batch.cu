@@ -34,6 +34,7 @@ struct moc_batch {
   int table_n = 0;
   cudaGraphExec_t exec = nullptr;
   cudaGraph_t graph = nullptr;
+  std::vector<int64_t> graph_key;       // per core (uploads, flags) when captured
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   int64_t launches = 0;
 };
@@ -60,8 +61,10 @@ int default_width(const moc_problem *p) {
   return w;
 }
 
-// Builds the per-core sweep arguments and the cost-ordered task list.
-int rebuild_tasks(moc_batch *b) {
+// Copies every core's sweep arguments to the device.  The batched kernel and a
+// captured graph read them there at run time, so they follow the cores' state
+// (an upload recomputes the fine-interval divisor check from the start heights).
+int upload_args(moc_batch *b) {
   const int n = (int)b->cores.size();
   std::vector<SweepArgs> args((size_t)n);
   for (int c = 0; c < n; ++c) {
@@ -70,6 +73,31 @@ int rebuild_tasks(moc_batch *b) {
     // the factor is 1 whenever no renormalisation is pending (see moc_reset_psi_scale)
     args[(size_t)c].psi_scale = p->psi_scale;
   }
+  MOC_CUDA_TRY(cudaMemcpy(b->d_args, args.data(), sizeof(SweepArgs) * (size_t)n, cudaMemcpyHostToDevice));
+  return MOC_OK;
+}
+
+// The captured iteration bakes in each core's work lists (rebuilt by an
+// upload) and update kernel (chosen by the mode flags).
+std::vector<int64_t> graph_key(const moc_batch *b) {
+  std::vector<int64_t> k;
+  for (const moc_problem *p : b->cores) {
+    k.push_back(p->uploads);
+    k.push_back(p->flags);
+  }
+  return k;
+}
+
+void drop_graph(moc_batch *b) {
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  b->exec = nullptr;
+  b->graph = nullptr;
+}
+
+// Builds the per-core sweep arguments and the cost-ordered task list.
+int rebuild_tasks(moc_batch *b) {
+  const int n = (int)b->cores.size();
   std::vector<int> order((size_t)n);
   std::iota(order.begin(), order.end(), 0);
   auto cost = [&](int c) {
@@ -87,14 +115,10 @@ int rebuild_tasks(moc_batch *b) {
   b->n_tasks = (int64_t)tasks.size();
   MOC_CUDA_TRY(cudaMalloc(&b->d_tasks, sizeof(int2) * (tasks.empty() ? 1 : tasks.size())));
   MOC_CUDA_TRY(cudaMemcpy(b->d_tasks, tasks.data(), sizeof(int2) * tasks.size(), cudaMemcpyHostToDevice));
-  MOC_CUDA_TRY(cudaMemcpy(b->d_args, args.data(), sizeof(SweepArgs) * (size_t)n, cudaMemcpyHostToDevice));
+  const int rc = upload_args(b);
+  if (rc != MOC_OK) return rc;
   MOC_CUDA_TRY(cudaMemcpy(b->d_tpw, b->tpw.data(), sizeof(int) * (size_t)n, cudaMemcpyHostToDevice));
-  if (b->exec) {
-    cudaGraphExecDestroy(b->exec);
-    cudaGraphDestroy(b->graph);
-    b->exec = nullptr;
-    b->graph = nullptr;
-  }
+  drop_graph(b);
   return MOC_OK;
 }
 
@@ -129,18 +153,23 @@ int batch_post(moc_batch *b) {
   return MOC_OK;
 }
 
-// A core uploaded since the batch last ran: its copies must land (and its
-// stream drain) before the batch stream reads its arrays.  A core that failed
-// or whose last upload was rejected is refused.
+// Before the batch stream reads the cores' arrays: each core's copies have
+// landed and its own stream has drained (work issued on a core since the batch
+// last ran), and the sweep arguments follow the cores' current state.  A core
+// that failed, whose last upload was rejected, or whose mode no longer matches
+// the batch is refused.
 int join_cores(moc_batch *b) {
+  MOC_CUDA_TRY(cudaStreamSynchronize(b->stream));   // no batch kernel reads the arguments
   for (moc_problem *p : b->cores) {
     if (p->status != MOC_OK || p->stale) return MOC_ERR_STATE;
-    if (p->n_chunks == 0) continue;
+    if (p->mode != b->mode || (p->mode == MOC_MODE_MIXED && (p->flags & MOC_FLAG_COMPENSATED)))
+      return MOC_ERR_STATE;
     int rc = moc_join_upload(p);
     if (rc != MOC_OK) return rc;
     MOC_CUDA_TRY(cudaStreamSynchronize(p->stream));
   }
-  return MOC_OK;
+  if (b->exec && graph_key(b) != b->graph_key) drop_graph(b);
+  return upload_args(b);
 }
 
 // After the batch stream has drained: every core's device error word, as a
@@ -247,6 +276,8 @@ int moc_batch_widths(const moc_batch *b, int *threads_per_track) {
 int moc_batch_autotune(moc_batch *b) {
   if (!b) return MOC_ERR_ARG;
   cudaSetDevice(b->device);
+  const int rc0 = join_cores(b);
+  if (rc0 != MOC_OK) return rc0;
   const int n = (int)b->cores.size();
   std::map<WidthKey, int> chosen;
   for (int c = 0; c < n; ++c) {
@@ -365,7 +396,11 @@ int moc_batch_power_iterations(moc_batch *b, int iters, int use_graph, double *m
       return rc != MOC_OK ? rc : MOC_ERR_CUDA;
     }
     b->graph = g;
-    if (cudaGraphInstantiate(&b->exec, g, 0) != cudaSuccess) return MOC_ERR_CUDA;
+    if (cudaGraphInstantiate(&b->exec, g, 0) != cudaSuccess) {
+      drop_graph(b);
+      return MOC_ERR_CUDA;
+    }
+    b->graph_key = graph_key(b);
   }
   cudaEventRecord(b->ev0, b->stream);
   for (int i = 0; i < iters && rc == MOC_OK; ++i) {

@@ -128,6 +128,7 @@ struct moc_problem {
   float *phi_in = nullptr;
   bool phi_fold_pending = false;
   bool stale = false;                            // rejected input: device state undefined
+  int64_t uploads = 0;                           // moc_upload calls that issued copies
   void *h_stage = nullptr;                       // pinned host staging of derived arrays
   cudaEvent_t stage_ev = nullptr;                // after the last copy from h_stage
   bool stage_pending = false;

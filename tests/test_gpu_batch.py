@@ -121,3 +121,39 @@ def test_batch_reports_a_cores_bad_source_id(gpu_available):
     finally:
         for s in solvers:
             s.close()
+
+
+def test_batch_graph_recaptured_after_an_upload(gpu_available):
+    """The captured iteration bakes in each core's update work lists.  After a
+    core is uploaded again with every source on one material (other work-list
+    sizes), the next graph call captures afresh: its results equal separate
+    runs of the new inputs (an upload does not reset the k_eff that the batch
+    chains on the device, so those runs start from it)."""
+    import simplemoc_gb300 as sm
+    from simplemoc_gb300.batch import Batch
+    specs = _specs()[:3]
+    hps = [sm.generate(s) for s in specs]
+    solvers = [sm.Solver(h, mode="plain") for h in hps]
+    new = hps[1].copy_state()
+    new.src_xs = np.zeros_like(hps[1].src_xs)
+    inputs = [hps[0], new, hps[2]]
+    try:
+        with Batch(solvers) as b:
+            b.power_iterations(2, graph=True)
+            keff0, _ = b.results()
+            for s, h in zip(solvers, inputs):
+                s.upload(h)
+            b.power_iterations(3, graph=True)
+            keff, _ = b.results()
+        n_done = 3 + 1                     # one eager iteration before the new capture
+        for c, (h, s) in enumerate(zip(inputs, solvers)):
+            with sm.Solver(h, mode="plain") as alone:
+                hist = alone.run(n_done, keff=float(keff0[c]))
+                ref = alone.download(fine_flux=True, fine_source=True, psi_f=True)
+            out = s.download(fine_flux=True, fine_source=True, psi_f=True)
+            assert abs(keff[c] - hist[-1][0]) <= 1e-5 * abs(hist[-1][0]), c
+            for k in ("fine_flux", "fine_source", "psi_f"):
+                assert rel_err(out[k], ref[k]) <= 1e-5, (c, k)
+    finally:
+        for s in solvers:
+            s.close()
