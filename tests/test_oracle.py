@@ -101,6 +101,28 @@ def test_port_matches_reference_fresh_problems(port, ref, lib, axial_exp, groups
         assert np.array_equal(a[k], b[k]), k
 
 
+@pytest.mark.parametrize("dims", [
+    # one group, one source, one 2D track of one segment, one stacked ray per polar angle
+    dict(n_groups=1, fai=3, cai=1, n_sources=1, n_tracks_2d=1, n_polar=2, z_stacked=1, n_seg=1),
+    dict(n_groups=3, fai=3, cai=2, n_sources=2, n_tracks_2d=2, n_polar=2, z_stacked=1, n_seg=2,
+         axial_exp=0),
+    # the most groups a batched core holds; more fine intervals and polar angles
+    dict(n_groups=128, fai=5, cai=4, n_sources=7, n_tracks_2d=2, n_polar=2, z_stacked=2, n_seg=5),
+    dict(n_groups=7, fai=12, cai=2, n_sources=5, n_tracks_2d=3, n_polar=6, z_stacked=5, n_seg=80),
+])
+def test_port_matches_reference_edge_sizes(port, ref, lib, dims):
+    """Degenerate and extreme sizes: the restatement equals the reference
+    objects bit for bit over three power iterations."""
+    import simplemoc_gb300 as sm
+    hp = sm.generate(sm.ProblemSpec(height=150.0, seed=77, **dims))
+    a, b = oracle.fresh_state(hp), oracle.fresh_state(hp)
+    ha = port.iterate(hp, a, 3)
+    hb = ref.iterate(hp, b, 3)
+    np.testing.assert_array_equal(np.asarray(ha), np.asarray(hb))
+    for k in a:
+        assert np.array_equal(a[k], b[k]), k
+
+
 def test_openmp_sweep_matches_serial_within_rounding(port, lib):
     """The locked OpenMP sweep (CPU timing path) computes the same tallies;
     only the order of additions differs."""
