@@ -204,7 +204,8 @@ int moc_batch_create(int n, moc_problem *const *problems, moc_batch **out) {
   for (moc_problem *p : b->cores) {
     // one launch: same device, mode, source order and (PLAIN) exponential table
     if (!p || p->status != MOC_OK || p->stale || p->device != b->device || p->mode != b->mode ||
-        (p->d.axial_exp == 2) != b->quad || p->ldg > 256 || p->mode == MOC_MODE_FP64 ||
+        (p->d.axial_exp == 2) != b->quad || p->ldg > 256 || p->n3d > INT32_MAX ||
+        p->mode == MOC_MODE_FP64 ||
         (p->mode == MOC_MODE_MIXED && (p->flags & MOC_FLAG_COMPENSATED)) ||
         p->d.table_n != p0->d.table_n || p->d.table_dx != p0->d.table_dx ||
         p->d.table_maxval != p0->d.table_maxval) {

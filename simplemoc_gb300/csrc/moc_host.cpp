@@ -279,12 +279,24 @@ int moc_host_validate(const moc_dims *d, const moc_host *h) {
 }
 
 int moc_host_validate_except_ids(const moc_dims *d, const moc_host *h) {
-  const int64_t G = d->n_groups, NS = d->n_sources, N3D = d->n_tracks_2d * d->n_polar * d->z_stacked;
+  const int64_t G = d->n_groups, NS = d->n_sources;
   const int64_t S = d->n_seg;
   if (G < 1 || d->fai < 1 || d->cai < 1 || d->decomp_ax < 1 || NS < 1 || d->n_sigt < 1 ||
       d->n_xs < 1 || d->n_tracks_2d < 1 || d->n_polar < 1 || d->n_polar > 64 ||
       d->z_stacked < 1 || S < 1)
     return MOC_ERR_ARG;
+  // Every array size must fit in 64-bit element and byte counts: products
+  // beyond 2^50 elements are rejected before any of them is formed in integers.
+  {
+    const double lim = 1125899906842624.0;   // 2^50
+    const double n2d = (double)d->n_tracks_2d, n3d = n2d * d->n_polar * d->z_stacked;
+    const double ldg = (double)G + 3.0;
+    if (n2d * d->n_polar * S > lim || n3d * S > lim || n3d * ldg > lim ||
+        (double)NS * d->fai * ldg > lim || (double)d->n_xs * G * G > lim ||
+        (double)d->n_sigt * ldg * 8 > lim || (double)d->table_n * 2 > lim)
+      return MOC_ERR_ARG;
+  }
+  const int64_t N3D = d->n_tracks_2d * d->n_polar * d->z_stacked;
   if (!(d->height > 0.0f) || NS > INT32_MAX) return MOC_ERR_ARG;
   if (d->axial_exp != 0 && d->axial_exp != 2) return MOC_ERR_ARG;   // src/solver.c:506-511
   if (d->axial_exp == 2 && d->fai < 3) return MOC_ERR_ARG;          // three rows are fitted

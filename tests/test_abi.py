@@ -117,6 +117,20 @@ def test_create_rejects_bad_inputs_before_device(lib, field, value):
     assert rc == 1        # MOC_ERR_ARG
 
 
+@pytest.mark.parametrize("field,value", [("n_tracks_2d", 1 << 45), ("n_groups", 1 << 30)])
+def test_create_rejects_sizes_beyond_64bit_counts(lib, field, value):
+    """Dimensions whose array lengths or byte counts would overflow 64-bit
+    integers are rejected before any array is read."""
+    import simplemoc_gb300 as sm
+    spec = sm.ProblemSpec(n_groups=8, n_sources=30, n_tracks_2d=4, n_polar=2, z_stacked=3,
+                          n_seg=10, seed=3)
+    hp = sm.generate(spec)
+    dims, host = hp.dims(), hp.host()
+    setattr(dims, field, value)
+    h = C.c_void_p()
+    assert lib.moc_create(C.byref(dims), C.byref(host), 0, C.byref(h)) == 1    # MOC_ERR_ARG
+
+
 def test_create_rejects_too_few_fine_intervals(lib):
     import simplemoc_gb300 as sm
     spec = sm.ProblemSpec(n_groups=8, fai=2, n_sources=30, n_tracks_2d=4, n_polar=2,
