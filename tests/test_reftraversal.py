@@ -49,6 +49,32 @@ def test_oracle_traversal_matches_reference_transport_sweep(port, ref, lib, axia
         assert np.array_equal(st_r["fine_flux"], st_o["fine_flux"])
 
 
+@pytest.mark.parametrize("case", [
+    # one 2D track of one segment, one stacked ray per polar angle, one group
+    dict(axial_exp=2, seed=21, n2d=1, n_polar=2, sep=40.0, groups=1, spt=1),
+    # two stacked rays per polar angle along a 200-segment 2D track
+    dict(axial_exp=2, seed=22, n2d=1, n_polar=2, sep=20.0, groups=3, spt=200),
+    # 400 stacked rays, 8 polar angles, flat source
+    dict(axial_exp=0, seed=23, n2d=3, n_polar=8, sep=0.1, groups=5, spt=5),
+    dict(axial_exp=2, seed=24, n2d=2, n_polar=4, sep=0.5, groups=128, spt=40),
+])
+def test_oracle_traversal_matches_reference_at_edge_sizes(port, ref, lib, case):
+    hp, geo = _case(**case)
+    rg = oracle.make_refgeo(geo)
+    op = oracle.make_problem(hp)
+    st_r, st_o = oracle.fresh_state(hp), oracle.fresh_state(hp)
+    z_r, z_o = geo.z_height.copy(), geo.z_height.copy()
+    for sweep in range(3):
+        LIBC.srand(500 + sweep)
+        n_r = ref.transport_sweep(hp, st_r, rg, z_r)
+        LIBC.srand(500 + sweep)
+        n_o = port.ref_sweep(op, rg, st_o["fine_source"], st_o["fine_flux"], st_o["psi_f"], z_o)
+        assert n_r == n_o > 0
+        assert np.array_equal(z_r, z_o)
+        assert np.array_equal(st_r["psi_f"], st_o["psi_f"])
+        assert np.array_equal(st_r["fine_flux"], st_o["fine_flux"])
+
+
 def test_traversal_with_given_ids_equals_libc_draws(port, lib):
     """ids[] in traversal order reproduce the rand() draws exactly."""
     hp, geo = _case(2, 9)
