@@ -100,3 +100,31 @@ def test_geometry_from_track_file(lib, tmp_path):
     assert g.p_weight.size == r.n_tracks_2d * 4 * 5
     gf = openmoc.to_geometry(r, n_polar=4, z_stacked=5, axial_z_sep=0.5, az_weight="file")
     assert np.array_equal(gf.az_weight, r.azim_weights[r.azim_index].astype(np.float32))
+
+
+def test_reader_rejects_every_truncation_and_survives_corruption(lib, tmp_path):
+    """Every proper prefix of a track file is rejected, and files with one
+    4-byte field overwritten (counts, ids or parts of doubles) are either read
+    or rejected, never read out of bounds."""
+    import struct
+
+    from simplemoc_gb300 import MocError, openmoc
+    path, t, _ = _file(tmp_path, seed=7, n_azimuthal=3, tracks_per_angle=2)
+    data = path.read_bytes()
+    bad = tmp_path / "bad.bin"
+    for cut in range(len(data)):
+        bad.write_bytes(data[:cut])
+        with pytest.raises(MocError):
+            openmoc.read(bad)
+    rng = np.random.default_rng(1)
+    values = [-1, 0, 1, 7, 1 << 20, -(1 << 30), (1 << 31) - 1]
+    for _ in range(1000):
+        b = bytearray(data)
+        off = int(rng.integers(0, len(data) - 4))
+        b[off:off + 4] = struct.pack("=i", values[int(rng.integers(len(values)))])
+        bad.write_bytes(bytes(b))
+        try:
+            r = openmoc.read(bad)
+        except MocError:
+            continue
+        assert r.seg_off[-1] == r.seg_len.size and np.all(np.diff(r.seg_off) >= 0)
