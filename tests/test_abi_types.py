@@ -103,3 +103,81 @@ def test_struct_mirrors_match_the_header(cname, pyname):
     want = _struct_fields(cname)
     got = [(n, _ctype_kind(t)) for n, t in getattr(L, pyname)._fields_]
     assert got == want
+
+
+# ---- the drop-in header (include/simplemoc_refabi.h) -------------------------
+
+REF_HEADER = ROOT / "include" / "simplemoc_refabi.h"
+REF_STRUCTS = {"moc_ref_input": "Input", "moc_ref_segment": "Segment",
+               "moc_ref_track2d": "Track2D", "moc_ref_track": "Track",
+               "moc_ref_source": "Source", "moc_ref_table": "Table",
+               "moc_ref_params": "Params", "moc_ref_commgrid": "CommGrid"}
+REF_SCALARS = dict(SCALARS, long="i64", bool="bool")
+
+
+def _ref_text():
+    text = re.sub(r"/\*.*?\*/", "", REF_HEADER.read_text(), flags=re.S)
+    # the serial build's layout: drop the OpenMP build's extra fields
+    return re.sub(r"#ifdef SIMPLEMOC_REF_OPENMP.*?#endif", "", text, flags=re.S)
+
+
+def _ref_kind(t: str, star: str) -> str:
+    if star:
+        return "ptr"
+    return f"struct:{t}" if t in REF_STRUCTS else REF_SCALARS[t]
+
+
+def _ref_ctype_kind(t) -> str:
+    for cname, pyname in REF_STRUCTS.items():
+        if getattr(t, "__name__", None) == pyname and issubclass(t, C.Structure):
+            return f"struct:{cname}"
+    if t is C.c_bool:
+        return "bool"
+    if t is C.c_long:
+        return "i64"
+    return _ctype_kind(t)
+
+
+@pytest.mark.parametrize("cname", sorted(REF_STRUCTS))
+def test_reference_struct_mirrors_match_the_drop_in_header(cname):
+    from simplemoc_gb300 import refabi
+    m = re.search(r"typedef\s+struct\s+" + cname + r"\s*\{(.*?)\}\s*" + cname + r"\s*;",
+                  _ref_text(), flags=re.S)
+    assert m, cname
+    want = []
+    for stmt in m.group(1).split(";"):
+        stmt = stmt.strip()
+        if not stmt:
+            continue
+        head, *rest = [s.strip() for s in stmt.split(",")]
+        t, star, name = re.match(r"([A-Za-z_][A-Za-z0-9_]*)\s*(\**)\s*([A-Za-z_][A-Za-z0-9_]*)$",
+                                 head).groups()
+        want.append((name, _ref_kind(t, star)))
+        for r in rest:
+            r_star, r_name = re.match(r"(\**)\s*([A-Za-z_][A-Za-z0-9_]*)$", r).groups()
+            want.append((r_name, _ref_kind(t, r_star)))
+    py = getattr(refabi, REF_STRUCTS[cname])
+    got = [(n, _ref_ctype_kind(t)) for n, t in py._fields_]
+    assert got == want
+
+
+def test_reference_entry_points_match_the_drop_in_header(lib):
+    from simplemoc_gb300 import refabi
+    lb = refabi.lib()
+    bad, seen = [], 0
+    for m in re.finditer(r"^\s*([A-Za-z_][A-Za-z0-9_]*\s*\**)\s*([A-Za-z_][A-Za-z0-9_]*)\s*"
+                         r"\(([^;{]*?)\)\s*;", _ref_text(), flags=re.M | re.S):
+        ret, name, params = m.group(1).strip(), m.group(2), m.group(3).strip()
+        kinds = []
+        if params not in ("", "void"):
+            for p in params.split(","):
+                t, star = re.match(r"\s*(?:const\s+)?([A-Za-z_][A-Za-z0-9_]*)\s*(\**)", p).groups()
+                kinds.append(_ref_kind(t, star))
+        r_t, r_star = re.match(r"([A-Za-z_][A-Za-z0-9_]*)\s*(\**)", ret).groups()
+        want = (_ref_kind(r_t, r_star), kinds)
+        fn = getattr(lb, name)
+        got = (_ref_ctype_kind(fn.restype), [_ref_ctype_kind(a) for a in fn.argtypes])
+        seen += 1
+        if got != want:
+            bad.append((name, want, got))
+    assert seen == 9 and not bad, (seen, bad)
