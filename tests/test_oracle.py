@@ -123,12 +123,13 @@ def test_port_matches_reference_edge_sizes(port, ref, lib, dims):
         assert np.array_equal(a[k], b[k]), k
 
 
-def test_openmp_sweep_matches_serial_within_rounding(port, lib):
+@pytest.mark.parametrize("axial_exp", [2, 0])
+def test_openmp_sweep_matches_serial_within_rounding(port, lib, axial_exp):
     """The locked OpenMP sweep (CPU timing path) computes the same tallies;
     only the order of additions differs."""
     import simplemoc_gb300 as sm
     spec = sm.ProblemSpec(n_groups=20, fai=5, cai=4, n_sources=60, n_tracks_2d=16, n_polar=4,
-                          z_stacked=8, n_seg=50, seed=5)
+                          z_stacked=8, n_seg=50, axial_exp=axial_exp, seed=5)
     hp = sm.generate(spec)
     op = oracle.make_problem(hp)
     a, b = oracle.fresh_state(hp), oracle.fresh_state(hp)
