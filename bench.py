@@ -211,6 +211,16 @@ def cpu_rate(spec, target_s: float, steps: int = 1):
     return rate, threads, sample, times
 
 
+METRIC = ("segment-group integrations/s per sweep, chosen vs plain @ FSR flux rel "
+          "err <=1e-5")
+
+
+def _workload(name: str, spec) -> str:
+    """The workload as both arms name it in config.workload."""
+    return (f"{name} problem: {spec.n_tracks_3d} 3D tracks x {spec.n_seg} segments x "
+            f"{spec.n_groups} groups, {spec.n_fsr} FSRs")
+
+
 def run_reference(args, spec):
     rank, world, _ = _dist()
     if rank != 0:
@@ -224,12 +234,15 @@ def run_reference(args, spec):
     sample_ints = rate * float(np.median(times))
     value = sample_ints / float(np.mean(timed))
     line = {
-        "impl": "reference", "metric": "segment-group integrations/s per sweep",
+        "impl": "reference", "metric": METRIC,
         "value": value, "unit": "integrations/s", "n_gpus": args.gpus, "steps": len(timed),
         "warmup": args.warmup, "ms_per_step": 1e3 * float(np.mean(timed)),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded)", "config": {"workload": f"{args.config} problem",
-                                                  "sample": sample},
+        "data": "synthetic (seeded)",
+        "config": {"workload": _workload(args.config, spec),
+                   "mode": "the reference's CPU sweep (PLAIN arithmetic), host cores",
+                   "step": "one sweep of a bounded sample of the workload",
+                   "sample": sample},
         "cpu_baseline": {"value": value, "unit": "integrations/s", "cores": threads,
                          "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": "integrations/s", "h2d_bytes_per_step": 0,
@@ -577,14 +590,11 @@ def main():
     traffic = _traffic_from_profiles() if args.config == "default" else None
     if rank == 0:
         line = {
-            "metric": "segment-group integrations/s per sweep, chosen vs plain @ FSR flux rel "
-                      "err <=1e-5",
+            "metric": METRIC,
             "value": value, "unit": "integrations/s", "n_gpus": world, "steps": K, "warmup": W,
             "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
-            "config": {"workload": f"{args.config} problem: {spec.n_tracks_3d} 3D tracks x "
-                                   f"{spec.n_seg} segments x {spec.n_groups} groups, "
-                                   f"{spec.n_fsr} FSRs",
+            "config": {"workload": _workload(args.config, spec),
                        "mode": "mixed", "step": "one power iteration",
                        "l2": "inputs larger than L2 (no flush)",
                        "parallelism": "replicas" if world > 1 else "single GPU"},
