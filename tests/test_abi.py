@@ -159,3 +159,18 @@ def test_solver_raises_loudly_without_gpu(lib):
                           n_seg=10, seed=3)
     with pytest.raises(sm.MocError):
         sm.Solver(sm.generate(spec))
+
+
+def test_algorithmic_bytes_of_the_default_problems(lib):
+    """The roofline numerator: 20 B per integration (12 B flat), 8 B per
+    track-group, 4 B per 3D segment id and 4 B per (2D segment, polar angle)
+    length.  The default problem moves 1.3239e12 B per sweep."""
+    import simplemoc_gb300 as sm
+    d = sm.CONFIGS["default"]
+    assert d.n_tracks_3d == 13_107_200 and d.n_seg == 50 and d.n_groups == 100
+    ints = d.n_tracks_3d * d.n_seg * d.n_groups
+    extra = 8 * d.n_tracks_3d * d.n_groups + 4 * d.n_tracks_3d * d.n_seg \
+        + 4 * d.n_tracks_2d * d.n_polar * d.n_seg
+    assert d.algorithmic_bytes() == 20 * ints + extra == 1_323_859_968_000
+    f = sm.CONFIGS["flat"]
+    assert f.axial_exp == 0 and f.algorithmic_bytes() == 12 * ints + extra
