@@ -239,6 +239,15 @@ int moc_set_sigma_t(moc_problem *p, const float *sigt);
 int moc_zero_state(moc_problem *p, int flux, int psi);
 int moc_get_fine_flux_device(moc_problem *p, float *phi);
 int moc_get_fine_flux64_device(moc_problem *p, double *phi);   /* FP64 mode */
+/* The handle's own scalar-flux storage (FP32, or FP64 in the FP64 mode):
+ * [NS*F][ldg] with ldg = G rounded up to a multiple of 4; the padding columns
+ * stay zero.  For a collective on the flux in place (the track-partitioned
+ * sweep sums the ranks' tallies with an all-reduce, the MPI_Allreduce of
+ * src/solver.c:1189-1196 widened from the fission rate to the flux): the
+ * caller orders its own access after moc_synchronize and finishes it before
+ * the handle's next call.  Any pending streamed upload is joined first. */
+int moc_fine_flux_storage(moc_problem *p, void **ptr, int64_t *n_elems, int32_t *ldg,
+                          int32_t *elem_bytes);
 
 /* ---- failure handling ---------------------------------------------------
  * Every call returns a status; after a CUDA failure, or after a kernel found an
@@ -329,11 +338,13 @@ int moc_batch_sweep(moc_batch *b);
 /* `iters` power iterations of every core (batched sweep, then each core's
  * renormalize_flux / update_sources / compute_keff with k_eff kept on the
  * device); use_graph captures one iteration as a CUDA graph and replays it.
- * Before it captures (its first call, and the first after an upload or a mode
- * flag change of a core) it runs one iteration without the graph, so that call
- * makes iters + 1 iterations.  *ms_total = device time of the `iters`
- * iterations (events on the batch stream).  Each call first waits for the
- * cores' own streams and refreshes their sweep arguments. */
+ * Every call makes exactly `iters` iterations: before it captures (its first
+ * call, and the first after an upload or a mode flag change of a core) it runs
+ * the first of them without the graph and replays the rest.  *ms_total =
+ * device time of the `iters` iterations (events on the batch stream; a call
+ * that captures also counts the time the device waits for the capture).  Each
+ * call first waits for the cores' own streams and refreshes their sweep
+ * arguments. */
 int moc_batch_power_iterations(moc_batch *b, int iters, int use_graph,
                                double *ms_total);
 /* Per-core k_eff and source residual of the last iteration. */
@@ -348,14 +359,17 @@ int64_t moc_batch_launch_count(const moc_batch *b);
  * moc_renormalize_flux on device buffers the caller owns, in the reference
  * layout (row stride n_groups):
  *   fine_flux [n_sources*fai*n_groups]  in/out   psi_f, psi_b [n_tracks_3d*n_groups] in/out
+ *     (psi_f and psi_b may be NULL when n_tracks_3d == 0)
  *   vol [n_sources], src_xs [n_sources], xs [n_xs*n_groups*3]  in
  *   norm_out: NULL or a device double[2] receiving (total fission rate, norm)
  * Launches on `stream` (a cudaStream_t; NULL = the legacy default stream) and
  * returns without waiting.  Its scratch is a static device array of
  * MOC_NOALLOC_SCRATCH_BYTES reserved on every GPU that loads the library until
- * the process exits; n_sources above MOC_NOALLOC_MAX_SOURCES is rejected with
- * MOC_ERR_ARG.  The first call on a device looks up the array's device address
- * (make it before any stream capture).  All calls share the one array: calls
+ * the process exits; n_sources above MOC_NOALLOC_MAX_SOURCES, or element
+ * counts above 2^50, are rejected with MOC_ERR_ARG.  The first call on a
+ * device looks up the array's device address (make it before any stream
+ * capture); a call that finds another context current on the device (after a
+ * cudaDeviceReset) looks it up again.  All calls share the one array: calls
  * whose kernels overlap on the GPU race. */
 #define MOC_NOALLOC_MAX_SOURCES (1 << 20)
 #define MOC_NOALLOC_SCRATCH_BYTES (8 * 1032 + 4 * MOC_NOALLOC_MAX_SOURCES)

@@ -14,7 +14,6 @@ simplemoc_gb300.problem.HostProblem (numpy, C-contiguous).
 from __future__ import annotations
 
 import ctypes as C
-import os
 import subprocess
 from pathlib import Path
 
@@ -22,8 +21,23 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 PORT_LIB = HERE / "_build" / "libmoc_oracle.so"
+# the same restatement built with the reference's timing flags (-Ofast
+# -ffast-math -ftree-vectorize -fopenmp): the timed CPU baseline, never a checker
+PORT_FAST_LIB = HERE / "_build" / "libmoc_oracle_fast.so"
 REF_LIB = HERE / "_ref" / "libref_harness.so"
-REF_SRC = Path(os.environ.get("SIMPLEMOC_REF_SRC", "/root/reference/src"))
+
+
+def ref_src() -> Path | None:
+    """The reference's src/ directory, as the oracle Makefile locates it
+    (SIMPLEMOC_REF_SRC overrides), or None where it is absent."""
+    try:
+        out = subprocess.run(["make", "-s", "-C", str(HERE), "print-ref-src"], check=True,
+                             capture_output=True, text=True).stdout.strip()
+    except (OSError, subprocess.CalledProcessError):
+        return None
+    p = Path(out) if out else None
+    return p if p is not None and (p / "solver.c").exists() else None
+
 
 f32p = C.POINTER(C.c_float)
 f64p = C.POINTER(C.c_double)
@@ -60,12 +74,22 @@ def make_refgeo(geo) -> OracleRefGeo:
 def build(reference: bool | None = None) -> None:
     """make -C oracle port [ref]; `ref` only where the reference sources exist."""
     targets = ["port"]
+    src = ref_src()
     if reference is None:
-        reference = (REF_SRC / "solver.c").exists()
-    if reference:
+        reference = src is not None
+    if reference and src is not None:
         targets.append("ref")
-    subprocess.run(["make", "-s", "-C", str(HERE), f"REF_SRC={REF_SRC}", *targets], check=True,
+    subprocess.run(["make", "-s", "-C", str(HERE), *targets, "port-fast"], check=True,
                    capture_output=True)
+
+
+def timing_flags() -> str:
+    """The compiler flags of the timing build (oracle/Makefile TFLAGS)."""
+    try:
+        return subprocess.run(["make", "-s", "-C", str(HERE), "print-timing-flags"], check=True,
+                              capture_output=True, text=True).stdout.strip()
+    except (OSError, subprocess.CalledProcessError):
+        return "unknown"
 
 
 def _p(a, t):
@@ -94,7 +118,11 @@ def make_problem(hp) -> OracleProblem:
 class Port:
     """The C restatement (moc_oracle.c)."""
 
-    def __init__(self, path: Path = PORT_LIB):
+    def __init__(self, path: Path = PORT_LIB, fast: bool = False):
+        """fast: the build with the reference's timing flags (for timing only:
+        its fast-math results are not the reference's bit for bit)."""
+        if fast:
+            path = PORT_FAST_LIB
         if not path.exists():
             build(reference=False)
         lib = C.CDLL(str(path))

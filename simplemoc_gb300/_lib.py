@@ -108,6 +108,9 @@ SIGNATURES = {
     "moc_set_sigma_t": (C.c_int, [C.c_void_p, f32p]),
     "moc_zero_state": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "moc_get_fine_flux_device": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "moc_fine_flux_storage": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p),
+                                        C.POINTER(C.c_int64), C.POINTER(C.c_int32),
+                                        C.POINTER(C.c_int32)]),
     "moc_get_fine_flux64_device": (C.c_int, [C.c_void_p, C.c_void_p]),
     "moc_adjoint_forward": (C.c_int, [C.c_void_p, C.c_int]),
     "moc_adjoint_backward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,

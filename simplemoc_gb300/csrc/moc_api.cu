@@ -1049,6 +1049,20 @@ int moc_get_fine_flux64_device(moc_problem *p, double *phi) {
   return rc == MOC_OK ? MOC_OK : fail(p, rc);
 }
 
+int moc_fine_flux_storage(moc_problem *p, void **ptr, int64_t *n_elems, int32_t *ldg,
+                          int32_t *elem_bytes) {
+  int rc = ready(p);
+  if (rc != MOC_OK) return rc;
+  if (!ptr) return MOC_ERR_ARG;
+  const bool fp64 = p->mode == MOC_MODE_FP64;
+  if (fp64 && !p->phi64) return MOC_ERR_STATE;
+  *ptr = fp64 ? static_cast<void *>(p->phi64) : static_cast<void *>(p->phi);
+  if (n_elems) *n_elems = p->nfsr * p->ldg;
+  if (ldg) *ldg = p->ldg;
+  if (elem_bytes) *elem_bytes = fp64 ? 8 : 4;
+  return MOC_OK;
+}
+
 // ---- adjoint ---------------------------------------------------------------
 
 int moc_adjoint_forward(moc_problem *p, int k_ckpt) {

@@ -374,18 +374,22 @@ int moc_batch_sweep(moc_batch *b) {
 // `iters` power iterations of every core: the batched sweep, then each core's
 // renormalize / update_sources / compute_keff, k_eff chained on the device.
 // With use_graph the iteration is captured once as a CUDA graph and replayed.
+// The call makes exactly `iters` iterations: before its first capture it runs
+// one of them eagerly (kernel attributes get set and every core reaches the
+// pending renormalisation that the graph replays) and replays the rest.
 int moc_batch_power_iterations(moc_batch *b, int iters, int use_graph, double *ms_total) {
   if (!b || iters < 1) return MOC_ERR_ARG;
   cudaSetDevice(b->device);
   int rc = join_cores(b);
   if (rc != MOC_OK) return rc;
+  int done = 0;
+  cudaEventRecord(b->ev0, b->stream);
   if (use_graph && !b->exec) {
-    // one eager iteration first: kernel attributes are set and every core has
-    // a pending renormalisation, the steady state the graph replays
     rc = batch_sweep(b);
     if (rc == MOC_OK) rc = batch_post(b);
     if (rc != MOC_OK) return rc;
-    MOC_CUDA_TRY(cudaStreamSynchronize(b->stream));
+    done = 1;
+    // capture records without executing; the eager iteration above runs on
     if (cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
       return MOC_ERR_CUDA;
     rc = batch_sweep(b);
@@ -403,8 +407,7 @@ int moc_batch_power_iterations(moc_batch *b, int iters, int use_graph, double *m
     }
     b->graph_key = graph_key(b);
   }
-  cudaEventRecord(b->ev0, b->stream);
-  for (int i = 0; i < iters && rc == MOC_OK; ++i) {
+  for (int i = done; i < iters && rc == MOC_OK; ++i) {
     if (use_graph) {
       if (cudaGraphLaunch(b->exec, b->stream) != cudaSuccess) rc = MOC_ERR_CUDA;
       b->launches++;

@@ -7,6 +7,7 @@
 // finalize kernel adds the partials in index order.  Scalars (norm factor,
 // keff, residual) stay on the device so that a whole power iteration can be
 // captured in a CUDA graph.
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
@@ -626,7 +627,10 @@ int moc_set_leakage(moc_problem *p, double leakage) {
 // name is only a stand-in for the device object.  Its device address is looked
 // up once per device with cudaGetSymbolAddress, below, while that device is
 // current; the first call on a device does this set-up, so make that first
-// call before any stream capture.
+// call before any stream capture.  The address belongs to the device's
+// context: the set-up records that context's unique id (cuCtxGetId) and is
+// repeated when a later call finds another context current (after a
+// cudaDeviceReset the module is loaded again, possibly at another address).
 // ---------------------------------------------------------------------------
 namespace {
 
@@ -639,21 +643,64 @@ static_assert(sizeof(g_renorm_scratch) == MOC_NOALLOC_SCRATCH_BYTES,
 
 constexpr int NOALLOC_MAX_DEVICES = 64;
 std::mutex g_scratch_mu;
-double *g_scratch_dev[NOALLOC_MAX_DEVICES] = {};
+struct ScratchSlot {
+  unsigned long long ctx_id;   // context the address was looked up in
+  double *addr;
+};
+ScratchSlot g_scratch_dev[NOALLOC_MAX_DEVICES] = {};
 
-// Device address of g_renorm_scratch on the current device (set-up once).
+// The two driver calls that identify the current context, resolved through
+// the runtime (the library does not link the driver library itself).
+using CtxGetCurrentFn = CUresult (*)(CUcontext *);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long *);
+CtxGetCurrentFn g_ctx_get_current = nullptr;
+CtxGetIdFn g_ctx_get_id = nullptr;
+
+// Unique id of the current context, 0 when none is current yet.
+int current_context_id(unsigned long long *id) {
+  *id = 0;
+  if (!g_ctx_get_current || !g_ctx_get_id) {
+    void *f1 = nullptr, *f2 = nullptr;
+    cudaDriverEntryPointQueryResult q1, q2;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault,
+                                         &q1) != cudaSuccess ||
+        cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) !=
+            cudaSuccess ||
+        q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess || !f1 || !f2) {
+      cudaGetLastError();
+      return MOC_ERR_CUDA;
+    }
+    g_ctx_get_current = reinterpret_cast<CtxGetCurrentFn>(f1);
+    g_ctx_get_id = reinterpret_cast<CtxGetIdFn>(f2);
+  }
+  CUcontext ctx = nullptr;
+  if (g_ctx_get_current(&ctx) != CUDA_SUCCESS) return MOC_ERR_CUDA;
+  if (ctx && g_ctx_get_id(ctx, id) != CUDA_SUCCESS) return MOC_ERR_CUDA;
+  return MOC_OK;
+}
+
+// Device address of g_renorm_scratch on the current device: looked up once per
+// device, and again only if the device's context has changed since.
 int scratch_address(int device, double **out) {
   std::lock_guard<std::mutex> lock(g_scratch_mu);
-  if (!g_scratch_dev[device]) {
+  unsigned long long id = 0;
+  int rc = current_context_id(&id);
+  if (rc != MOC_OK) return rc;
+  ScratchSlot &slot = g_scratch_dev[device];
+  if (!slot.addr || id == 0 || slot.ctx_id != id) {
     void *ptr = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&ptr, g_renorm_scratch);
     if (e != cudaSuccess || ptr == nullptr) {
       cudaGetLastError();
       return MOC_ERR_CUDA;
     }
-    g_scratch_dev[device] = static_cast<double *>(ptr);
+    // the look-up makes the device's primary context current if none was
+    rc = current_context_id(&id);
+    if (rc != MOC_OK) return rc;
+    slot.addr = static_cast<double *>(ptr);
+    slot.ctx_id = id;
   }
-  *out = g_scratch_dev[device];
+  *out = slot.addr;
   return MOC_OK;
 }
 
@@ -664,9 +711,17 @@ extern "C" int moc_renormalize_flux_noalloc(float *fine_flux, float *psi_f, floa
                                             const float *xs, int64_t n_sources, int32_t fai,
                                             int32_t n_groups, int64_t n_tracks_3d,
                                             double *norm_out, void *stream) {
-  if (!fine_flux || !psi_f || !psi_b || !vol || !src_xs || !xs) return MOC_ERR_ARG;
+  if (!fine_flux || !vol || !src_xs || !xs) return MOC_ERR_ARG;
   if (n_sources < 1 || fai < 1 || n_groups < 1 || n_tracks_3d < 0) return MOC_ERR_ARG;
+  if (n_tracks_3d > 0 && (!psi_f || !psi_b)) return MOC_ERR_ARG;  // no tracks: psi may be NULL
   if (n_sources > MOC_NOALLOC_MAX_SOURCES) return MOC_ERR_ARG;   // scratch holds one float per source
+  {
+    // element counts must fit 64-bit integers: products beyond 2^50 are
+    // rejected before they are formed (the bound of the handle's validation)
+    const double lim = 1125899906842624.0;   // 2^50
+    if ((double)n_sources * fai * n_groups > lim || (double)n_tracks_3d * n_groups > lim)
+      return MOC_ERR_ARG;
+  }
   int device = 0;
   if (cudaGetDevice(&device) != cudaSuccess) {
     cudaGetLastError();

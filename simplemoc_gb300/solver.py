@@ -162,6 +162,20 @@ class Solver:
     def launch_count(self) -> int:
         return int(self._lib.moc_launch_count(self._h))
 
+    def zero_state(self, flux: bool = True, psi: bool = False) -> None:
+        """Zeroes the scalar flux and/or the angular flux (moc_zero_state)."""
+        L.check(self._lib.moc_zero_state(self._h, int(flux), int(psi)), "moc_zero_state")
+
+    def flux_storage(self) -> dict:
+        """The handle's scalar-flux storage on the device (moc_fine_flux_storage):
+        pointer, element count, row stride and element size.  Access it only
+        after synchronize() and before the handle's next call."""
+        ptr, n, ldg, eb = C.c_void_p(), C.c_int64(), C.c_int32(), C.c_int32()
+        L.check(self._lib.moc_fine_flux_storage(self._h, C.byref(ptr), C.byref(n), C.byref(ldg),
+                                                C.byref(eb)), "moc_fine_flux_storage")
+        return {"ptr": int(ptr.value or 0), "n": int(n.value), "ldg": int(ldg.value),
+                "elem_bytes": int(eb.value)}
+
     def device_bytes(self) -> int:
         return int(self._lib.moc_device_bytes(self._h))
 

@@ -36,7 +36,7 @@ def port():
 def ref():
     import oracle
     if not oracle.Reference.available():
-        if (oracle.REF_SRC / "solver.c").exists():
+        if oracle.ref_src() is not None:
             oracle.build(reference=True)
     if not oracle.Reference.available():
         pytest.skip("reference objects not built (reference sources absent)")

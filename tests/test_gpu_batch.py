@@ -64,10 +64,10 @@ def test_batched_power_iterations_match_separate_runs(gpu_available, graph):
         b.power_iterations(iters, graph=graph)
         keff, res = b.results()
     for c, (h, s) in enumerate(zip(hps, solvers)):
-        # the graph path runs one eager iteration before its first capture
-        n_done = iters + (1 if graph else 0)
+        # exactly `iters` iterations, with or without the graph (its first
+        # call runs one of them eagerly before capturing)
         with sm.Solver(h, mode="plain") as alone:
-            hist = alone.run(n_done)
+            hist = alone.run(iters)
             ref = alone.download(fine_flux=True, fine_source=True, psi_f=True)
         out = s.download(fine_flux=True, fine_source=True, psi_f=True)
         assert abs(keff[c] - hist[-1][0]) <= 1e-5 * abs(hist[-1][0]), c

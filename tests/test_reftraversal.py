@@ -96,8 +96,8 @@ def test_reference_driver_links_against_the_library(tmp_path, lib):
     against libsimplemoc_gb300.so in place of solver.o, unchanged, and the
     driver runs to its summary; without a GPU every solver call reports
     MOC_ERR_NO_DEVICE through moc_ref_status and keff is NaN (no CPU fallback)."""
-    src = oracle.REF_SRC
-    if not (src / "main.c").exists():
+    src = oracle.ref_src()
+    if src is None or not (src / "main.c").exists():
         pytest.skip("reference sources not mounted")
     libdir = ROOT / "simplemoc_gb300"
     exe = tmp_path / "SimpleMOC_gpu"
