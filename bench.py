@@ -62,6 +62,11 @@ def _args():
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0,
                     help="target CPU time of one reference-arm sample")
+    ap.add_argument("--accuracy-iters", type=int, default=20,
+                    help="power iterations of the accuracy comparison against the FP64 mode "
+                         "(on the whole workload)")
+    ap.add_argument("--no-compensated", action="store_true",
+                    help="skip timing MIXED with compensated tallies")
     ap.add_argument("--launch", default=None, metavar="TPW,CPL",
                     help="fixed sweep launch shape (threads per track, chunks per thread) "
                          "instead of the autotuner's")
@@ -167,6 +172,14 @@ def _pinned_alloc():
     return alloc
 
 
+def _timing_port():
+    """The oracle's restatement built with the reference's own timing flags
+    (-Ofast -ffast-math -ftree-vectorize -fopenmp, src/Makefile:77,102-113),
+    and those flags."""
+    import oracle
+    return oracle.Port(fast=True), oracle.timing_flags()
+
+
 def _cpu_sample_spec(spec, target_s: float, port, threads: int):
     """A sample of the workload for the CPU: the same sources, groups, polar
     angles, stacked rays and segments, over fewer 2D tracks, sized to take about
@@ -193,7 +206,7 @@ def cpu_rate(spec, target_s: float, steps: int = 1):
     reference's OpenMP build) on a bounded sample of the workload."""
     import oracle
     import simplemoc_gb300 as sm
-    port = oracle.Port()
+    port, flags = _timing_port()
     threads = port.lib.oracle_omp_max_threads()
     sspec = _cpu_sample_spec(spec, target_s, port, threads)
     hp = sm.generate(sspec)
@@ -207,8 +220,9 @@ def cpu_rate(spec, target_s: float, steps: int = 1):
     rate = sspec.integrations_per_sweep / float(np.median(times))
     sample = (f"OpenMP sweep of {sspec.n_tracks_2d} of {spec.n_tracks_2d} 2D tracks (all "
               f"{spec.n_polar} polar x {spec.z_stacked} stacked 3D tracks each, "
-              f"{sspec.integrations_per_sweep:.3e} integrations) over the full source storage")
-    return rate, threads, sample, times
+              f"{sspec.integrations_per_sweep:.3e} integrations) over the full source storage; "
+              f"compiled {flags}")
+    return rate, threads, sample, times, flags
 
 
 METRIC = ("segment-group integrations/s per sweep, chosen vs plain @ FSR flux rel "
@@ -221,6 +235,60 @@ def _workload(name: str, spec) -> str:
             f"{spec.n_groups} groups, {spec.n_fsr} FSRs")
 
 
+CONTRACT = 1e-5          # FSR flux relative error against the FP64 mode
+KEFF_CONTRACT = 1e-6
+
+
+def flux_errors(a, ref, G: int) -> dict:
+    """Relative errors of a scalar flux against the FP64 one: normwise
+    (max |a - ref| / max |ref|), per FSR (each FSR's group vector in the max
+    norm: max_g |a - ref| / max_g |ref|), and per element (FSR x group)."""
+    a = np.asarray(a, dtype=np.float64)
+    ref = np.asarray(ref, dtype=np.float64)
+    d = np.abs(a - ref)
+    r = np.abs(ref)
+    fsr_den = r.reshape(-1, G).max(1)
+    per_fsr = d.reshape(-1, G).max(1)[fsr_den > 0] / fsr_den[fsr_den > 0]
+    nz = r > 0
+    per_el = d[nz] / r[nz]
+    qs = (0.5, 0.99, 0.999, 0.9999)
+    return {
+        "normwise": float(d.max() / r.max()),
+        "per_fsr_max": float(per_fsr.max()),
+        "per_fsr_quantiles": {str(q): float(np.quantile(per_fsr, q)) for q in qs},
+        "per_fsr_frac_within_contract": float((per_fsr <= CONTRACT).mean()),
+        "per_element_max": float(per_el.max()),
+        "per_element_quantiles": {str(q): float(np.quantile(per_el, q)) for q in qs},
+    }
+
+
+def accuracy_block(spec, device: int, iters: int) -> dict:
+    """Every mode against the FP64 mode (the same formulas in double with an
+    exact 1 - exp(-tau)) on the whole workload over `iters` power iterations:
+    FSR flux errors normwise, per FSR and per element, and the k_eff error."""
+    import simplemoc_gb300 as sm
+    hp = sm.generate(spec, with_state=False)
+    t0 = time.perf_counter()
+    with sm.Solver(hp, device=device, mode="fp64") as s64:
+        h64 = s64.run(iters)
+        p64 = s64.download64(fine_flux=True)["fine_flux"]
+    out = {"workload": f"all {spec.n_tracks_3d} 3D tracks, {iters} power iterations",
+           "reference": "FP64 mode", "fp64_seconds": time.perf_counter() - t0,
+           "contract": {"fsr_flux_rel_err": CONTRACT, "keff_rel_err": KEFF_CONTRACT}}
+    k64 = h64[-1][0]
+    for name, mode, comp in (("mixed", "mixed", False), ("mixed_compensated", "mixed", True),
+                             ("plain", "plain", False)):
+        with sm.Solver(hp, device=device, mode=mode, compensated=comp) as s:
+            h = s.run(iters)
+            ph = s.download(fine_flux=True, fine_source=False, psi_f=False)["fine_flux"]
+        e = flux_errors(ph, p64, spec.n_groups)
+        e["keff_rel_err"] = abs(h[-1][0] - k64) / abs(k64)
+        e["normwise_within_contract"] = (e["normwise"] <= CONTRACT
+                                         and e["keff_rel_err"] <= KEFF_CONTRACT)
+        out[name] = e
+    return out
+
+
 def run_reference(args, spec):
     rank, world, _ = _dist()
     if rank != 0:
@@ -228,8 +296,8 @@ def run_reference(args, spec):
     import oracle
     kind = "reference" if oracle.Reference.available() else "port"
     # warm-up + timed steps, each one bounded sample sweep
-    rate, threads, sample, times = cpu_rate(spec, args.cpu_seconds / 2,
-                                            steps=max(1, args.steps) + max(0, args.warmup))
+    rate, threads, sample, times, flags = cpu_rate(
+        spec, args.cpu_seconds / 2, steps=max(1, args.steps) + max(0, args.warmup))
     timed = times[max(0, args.warmup):] or times
     sample_ints = rate * float(np.median(times))
     value = sample_ints / float(np.mean(timed))
@@ -242,15 +310,16 @@ def run_reference(args, spec):
         "config": {"workload": _workload(args.config, spec),
                    "mode": "the reference's CPU sweep (PLAIN arithmetic), host cores",
                    "step": "one sweep of a bounded sample of the workload",
-                   "sample": sample},
+                   "sample": sample, "compiler_flags": flags},
         "cpu_baseline": {"value": value, "unit": "integrations/s", "cores": threads,
-                         "kind": "port", "sample": sample},
+                         "kind": "port", "sample": sample, "compiler_flags": flags},
         "e2e": {"value": value, "unit": "integrations/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
         "note": ("the reference's own sweep code is C with a time-seeded RNG; the timed CPU "
                  "path is the oracle's restatement of attenuate_fluxes with the reference's "
-                 "per-region OpenMP locks, pinned bit-for-bit to the reference objects in "
-                 "this repository's tests"),
+                 "per-region OpenMP locks (pinned bit-for-bit to the reference objects in "
+                 "this repository's tests when built with the results flags), built here "
+                 "with the reference's own timing flags"),
     }
     if kind == "reference":
         line["note"] += "; reference objects available but the sweep is timed on the port"
@@ -514,17 +583,28 @@ def main():
     rp = solver.time_power_iterations(K)
     plain_value = ints * K / (rp["ms_total"] / 1e3)
     plain_sweep_ms = rp["ms_sweeps"] / K
+
+    # ---- MIXED with compensated tallies ------------------------------------------
+    comp = None
+    if not args.no_compensated:
+        solver.set_mode("mixed", compensated=True)
+        shapes["mixed_compensated"] = tune()
+        solver.time_power_iterations(1)
+        rc_ = solver.time_power_iterations(K)
+        comp = {"value": ints * K / (rc_["ms_total"] / 1e3), "unit": "integrations/s",
+                "sweep_ms": rc_["ms_sweeps"] / K}
     solver.set_mode("mixed")
     if args.launch:
         solver.set_launch(*args.launch)
     else:
         solver.autotune(measure=False)
+    phases = solver.time_phases(3)["phases_ms"]
 
     # ---- end to end through the C ABI with host buffers ------------------------
     e2e = None
     if e2e_on:
         out = {"fine_flux": alloc((spec.n_fsr * spec.n_groups,), np.float32)}
-        steps = 9                       # ~0.25 s each; nine for a steadier median
+        steps = K
         solver.upload(hp)
         solver.power_iteration(1.0)
         solver.download(fine_flux=True, fine_source=False, psi_f=False, out=out)
@@ -554,35 +634,18 @@ def main():
                "d2h_bytes_per_step": int(out["fine_flux"].nbytes + 16),
                "ms_steps": [round(1e3 * x, 2) for x in step_s]}
 
-    # ---- accuracy of the chosen mode against FP64 on a reduced problem ---------
+    # ---- accuracy of every mode against the FP64 mode, on the whole workload ---
     accuracy = None
     if not args.no_accuracy and rank == 0:
-        aspec = spec.with_(n_tracks_2d=max(64, spec.n_tracks_2d // 64))
-        ahp = sm.generate(aspec)
-        with sm.Solver(ahp, device=local, mode="fp64") as s64, \
-                sm.Solver(ahp, device=local, mode="mixed") as smx, \
-                sm.Solver(ahp, device=local, mode="plain") as spl:
-            h64 = s64.run(3)
-            hmx = smx.run(3)
-            hpl = spl.run(3)
-            p64 = s64.download64(fine_flux=True)["fine_flux"]
-            pmx = smx.download(fine_flux=True, fine_source=False, psi_f=False)["fine_flux"]
-            ppl = spl.download(fine_flux=True, fine_source=False, psi_f=False)["fine_flux"]
-        den = np.abs(p64).max()
-        accuracy = {
-            "sample": f"{aspec.n_tracks_2d} of {spec.n_tracks_2d} 2D tracks, 3 power iterations",
-            "mixed_phi_rel_err_vs_fp64": float(np.abs(pmx - p64).max() / den),
-            "mixed_keff_rel_err_vs_fp64": abs(hmx[-1][0] - h64[-1][0]) / abs(h64[-1][0]),
-            "plain_phi_rel_err_vs_fp64": float(np.abs(ppl - p64).max() / den),
-            "plain_keff_rel_err_vs_fp64": abs(hpl[-1][0] - h64[-1][0]) / abs(h64[-1][0]),
-        }
+        solver.close()                  # room for the FP64 state
+        accuracy = accuracy_block(spec, local, max(1, args.accuracy_iters))
 
     # ---- CPU baseline (rank 0, N = 1 only) -------------------------------------
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        rate, threads, sample, _ = cpu_rate(spec, args.cpu_seconds)
+        rate, threads, sample, _, flags = cpu_rate(spec, args.cpu_seconds)
         cpu = {"value": rate, "unit": "integrations/s", "cores": threads, "kind": "port",
-               "sample": sample}
+               "sample": sample, "compiler_flags": flags}
 
     peak, peak_kind = _peaks()
     alg_bytes = spec.algorithmic_bytes()
@@ -601,6 +664,8 @@ def main():
             "plain": {"value": plain_value, "unit": "integrations/s",
                       "sweep_ms": plain_sweep_ms},
             "chosen_vs_plain": value / world / plain_value,
+            "compensated": comp,
+            "phases_ms": {k: v / 3 for k, v in phases.items()},
             "sweep_ms": sweep_ms, "keff": r["keff"], "launch_shape": shapes,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,

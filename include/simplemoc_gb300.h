@@ -61,6 +61,24 @@ extern "C" {
  * (split TF32, FP32 accumulation; up to 104 groups); this flag keeps it on the
  * CUDA cores instead. */
 #define MOC_FLAG_SIMT_UPDATE 0x2
+/* PLAIN or MIXED: deterministic-order tallies.  The sweep records every
+ * segment's contribution instead of adding it; the contributions of each FSR
+ * are then added to the scalar flux in the serial order of the tracks and
+ * their segments (track t before t + 1, segment n before n + 1), the order of
+ * the reference's serial sweep over the same tracks (its tally
+ * fine_flux[g] += ..., src/solver.c:212-228).  The flux is then the same in
+ * every run, and in PLAIN equal bit for bit to the serial reference's.  The
+ * records take up to ~2 GiB of device memory, in chunks of whole 2D tracks;
+ * the sweep takes a few times longer.  Explicit segment streams, up to 256
+ * groups, not with MOC_FLAG_COMPENSATED (MOC_ERR_UNSUPPORTED). */
+#define MOC_FLAG_DETERMINISTIC 0x4
+/* FP64 only: FP64 arithmetic on state stored as FP32 values.  The scalar
+ * flux and angular flux are rounded to FP32 after each sweep and
+ * renormalisation, the fine source after each update, as an FP32-state solver
+ * stores them.  Its distance from the plain FP64 mode is the error floor that
+ * FP32 storage of the state alone sets (a yardstick for MIXED, which stores its
+ * state in FP32). */
+#define MOC_FLAG_FP32_STATE 0x8
 
 /* ---- problem description ---------------------------------------------- */
 typedef struct moc_dims {
@@ -226,6 +244,21 @@ int moc_time_sweep(moc_problem *p, int iters, double *ms_per_sweep);
  * launching stream) and the final k_eff and residual. */
 int moc_time_power_iterations(moc_problem *p, int iters, double *ms_total,
                               double *ms_sweeps, double *keff, double *residual);
+/* Per-phase device times of `iters` power iterations, under the phases of the
+ * reference's results summary (src/main.c:103-113): phase_ms[MOC_N_PHASES],
+ * milliseconds summed over the iterations, from events on the launching
+ * stream.  The exchange phase is 0 on one device (the track-partitioned
+ * sweep's all-reduce runs outside the handle).  update_sources and
+ * compute_keff run as the reference's two calls, k_eff chained on the device
+ * (moc_power_iteration fuses their passes over the flux). */
+#define MOC_PHASE_SWEEP       0   /* Transport Sweep Time         */
+#define MOC_PHASE_EXCHANGE    1   /* Domain Flux Exchange Time    */
+#define MOC_PHASE_RENORMALIZE 2   /* Flux Renormalization Time    */
+#define MOC_PHASE_UPDATE      3   /* Update Source Time           */
+#define MOC_PHASE_KEFF        4   /* K-Effective Calc Time        */
+#define MOC_N_PHASES          5
+int moc_time_phases(moc_problem *p, int iters, double *phase_ms, double *keff,
+                    double *residual);
 /* Number of kernels the library has launched on this handle so far. */
 int64_t moc_launch_count(const moc_problem *p);
 

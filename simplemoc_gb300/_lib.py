@@ -26,9 +26,14 @@ MOC_MODE_MIXED = 1
 MOC_MODE_FP64 = 2
 MOC_FLAG_COMPENSATED = 0x1
 MOC_FLAG_SIMT_UPDATE = 0x2
+MOC_FLAG_DETERMINISTIC = 0x4
+MOC_FLAG_FP32_STATE = 0x8
 MOC_FAULT_CUDA = 0
 MOC_FAULT_DEVICE_INPUT = 1
 MOC_FAULT_DEVICE_TIMEOUT = 2
+# phases of the reference's results summary (src/main.c:103-113)
+PHASE_NAMES = ("Transport Sweep", "Domain Flux Exchange", "Flux Renormalization",
+               "Update Source", "K-Effective Calc")
 
 f32p = C.POINTER(C.c_float)
 f64p = C.POINTER(C.c_double)
@@ -108,6 +113,7 @@ SIGNATURES = {
     "moc_set_sigma_t": (C.c_int, [C.c_void_p, f32p]),
     "moc_zero_state": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
     "moc_get_fine_flux_device": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "moc_time_phases": (C.c_int, [C.c_void_p, C.c_int, f64p, f64p, f64p]),
     "moc_fine_flux_storage": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p),
                                         C.POINTER(C.c_int64), C.POINTER(C.c_int32),
                                         C.POINTER(C.c_int32)]),

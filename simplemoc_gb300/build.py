@@ -25,7 +25,7 @@ LIB = PKG / "libsimplemoc_gb300.so"
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 CU_SOURCES = ["moc_api.cu", "moc_sweep.cu", "moc_post.cu", "moc_refabi.cu", "moc_batch.cu",
-              "moc_update_tc.cu"]
+              "moc_update_tc.cu", "moc_determ.cu"]
 CPP_SOURCES = ["moc_host.cpp", "moc_openmoc.cpp"]
 
 
@@ -77,7 +77,7 @@ def build(verbose: bool = False) -> Path:
         # -Bsymbolic: calls inside the library bind to its own definitions even when
         # another loaded object exports the same reference entry-point names
         _run([_nvcc(), ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-Xcompiler", "-fopenmp",
-              "-Xlinker", "-Bsymbolic", "-lgomp"])
+              "-Xlinker", "-Bsymbolic", "-lgomp", "-ldl"])
         os.replace(tmp, LIB)
     return LIB
 

@@ -66,6 +66,23 @@ int dalloc(moc_problem *p, T **ptr, int64_t count) {
   return MOC_OK;
 }
 
+}  // namespace
+
+int moc_dev_alloc(moc_problem *p, void **ptr, int64_t bytes) {
+  unsigned char *d = nullptr;
+  const int rc = dalloc(p, &d, bytes);
+  *ptr = d;
+  return rc;
+}
+
+void moc_dev_free(moc_problem *p, void *ptr, int64_t bytes) {
+  if (!ptr) return;
+  cudaFree(ptr);
+  p->bytes -= bytes > 0 ? bytes : 1;
+}
+
+namespace {
+
 template <typename T>
 void dfree(T *&ptr) {
   if (ptr) cudaFree(ptr);
@@ -343,6 +360,7 @@ int upload_all(moc_problem *p, const moc_host *h, bool stream_tracks) {
 }
 
 void release(moc_problem *p) {
+  moc_det_release(p);
   dfree(p->seg_ds); dfree(p->seg_src); dfree(p->weight); dfree(p->z0); dfree(p->mu);
   dfree(p->src_sigt); dfree(p->src_xs); dfree(p->vol); dfree(p->coef); dfree(p->xs);
   dfree(p->scatter_t); dfree(p->table); dfree(p->q); dfree(p->phi); dfree(p->phi_lo);
@@ -426,7 +444,11 @@ int read_scalars(moc_problem *p, double *out) {
 int sweep_impl(moc_problem *p) {
   const bool had_pending = p->psi_pending && p->mode != MOC_MODE_FP64;
   int rc = MOC_OK;
-  if (p->n_chunks > 0 && p->mode != MOC_MODE_FP64) {
+  if (p->flags & MOC_FLAG_DETERMINISTIC) {
+    // the uploaded flux lands first: the tallies are added on top of it in order
+    rc = moc_join_upload(p);
+    if (rc == MOC_OK) rc = moc_det_sweep(p);
+  } else if (p->n_chunks > 0 && p->mode != MOC_MODE_FP64) {
     // sweep each chunk of 2D tracks once its copy has landed
     int64_t i0 = 0;
     for (int k = 0; k < p->n_chunks && rc == MOC_OK; ++k) {
@@ -443,6 +465,10 @@ int sweep_impl(moc_problem *p) {
   if (had_pending) {                   // the sweep applied it
     p->psi_pending = false;
     rc = moc_reset_psi_scale(p);
+    if (rc != MOC_OK) return fail(p, rc);
+  }
+  if (p->mode == MOC_MODE_FP64) {
+    rc = moc_round_state_fp32(p, true, true, false);
     if (rc != MOC_OK) return fail(p, rc);
   }
   if (p->mode == MOC_MODE_MIXED && (p->flags & MOC_FLAG_COMPENSATED) && p->phi_lo) {
@@ -637,6 +663,7 @@ int moc_destroy(moc_problem *p) {
 }
 
 int moc_upload(moc_problem *p, const moc_host *host) {
+  MOC_NVTX_RANGE("moc_upload");
   if (!p) return MOC_ERR_ARG;
   if (p->status != MOC_OK) return MOC_ERR_STATE;
   if (!host) return MOC_ERR_ARG;
@@ -669,6 +696,7 @@ int moc_upload(moc_problem *p, const moc_host *host) {
 }
 
 int moc_download(moc_problem *p, float *fine_flux, float *fine_source, float *psi_f, float *psi_b) {
+  MOC_NVTX_RANGE("moc_download");
   int rc = ready(p);
   if (rc != MOC_OK) return rc;
   if (psi_f && p->psi_pending) {
@@ -710,7 +738,13 @@ int moc_set_mode(moc_problem *p, int mode, int flags) {
   int rc = ready(p);
   if (rc != MOC_OK) return rc;
   if (mode != MOC_MODE_PLAIN && mode != MOC_MODE_MIXED && mode != MOC_MODE_FP64) return MOC_ERR_ARG;
-  if (flags & ~(MOC_FLAG_COMPENSATED | MOC_FLAG_SIMT_UPDATE)) return MOC_ERR_ARG;
+  if (flags & ~(MOC_FLAG_COMPENSATED | MOC_FLAG_SIMT_UPDATE | MOC_FLAG_DETERMINISTIC |
+                MOC_FLAG_FP32_STATE))
+    return MOC_ERR_ARG;
+  if ((flags & MOC_FLAG_FP32_STATE) && mode != MOC_MODE_FP64) return MOC_ERR_UNSUPPORTED;
+  if ((flags & MOC_FLAG_DETERMINISTIC) &&
+      (mode == MOC_MODE_FP64 || (flags & MOC_FLAG_COMPENSATED) || p->ldg > 256))
+    return MOC_ERR_UNSUPPORTED;
   if (p->psi_pending) {
     rc = moc_psi_materialize(p);
     if (rc != MOC_OK) return fail(p, rc);
@@ -812,6 +846,7 @@ int moc_autotune(moc_problem *p, int64_t n_tracks, int *threads_per_track,
 }
 
 int moc_transport_sweep(moc_problem *p, int64_t *segments_processed) {
+  MOC_NVTX_RANGE("transport_sweep");
   int rc = usable(p);
   if (rc != MOC_OK) return rc;
   cudaSetDevice(p->device);
@@ -822,6 +857,7 @@ int moc_transport_sweep(moc_problem *p, int64_t *segments_processed) {
 }
 
 int moc_renormalize_flux(moc_problem *p) {
+  MOC_NVTX_RANGE("renormalize_flux");
   int rc = ready(p);
   if (rc != MOC_OK) return rc;
   cudaSetDevice(p->device);
@@ -830,6 +866,7 @@ int moc_renormalize_flux(moc_problem *p) {
 }
 
 int moc_update_sources(moc_problem *p, double keff, double *residual) {
+  MOC_NVTX_RANGE("update_sources");
   int rc = ready(p);
   if (rc != MOC_OK) return rc;
   if (!(keff != 0.0)) return MOC_ERR_ARG;
@@ -846,6 +883,7 @@ int moc_update_sources(moc_problem *p, double keff, double *residual) {
 }
 
 int moc_compute_keff(moc_problem *p, double leakage, double *keff) {
+  MOC_NVTX_RANGE("compute_keff");
   int rc = ready(p);
   if (rc != MOC_OK) return rc;
   cudaSetDevice(p->device);
@@ -859,6 +897,7 @@ int moc_compute_keff(moc_problem *p, double leakage, double *keff) {
 }
 
 int moc_power_iteration(moc_problem *p, double keff_in, double *keff_out, double *residual) {
+  MOC_NVTX_RANGE("power_iteration");
   int rc = usable(p);
   if (rc != MOC_OK) return rc;
   if (!(keff_in != 0.0)) return MOC_ERR_ARG;
@@ -892,10 +931,16 @@ int moc_time_sweep(moc_problem *p, int iters, double *ms_per_sweep) {
   cudaSetDevice(p->device);
   double total = 0.0;
   for (int i = 0; i < iters; ++i) {
+    const bool had_pending = p->psi_pending && p->mode != MOC_MODE_FP64;
     if (cudaEventRecord(p->ev0, p->stream) != cudaSuccess) return fail(p, MOC_ERR_CUDA);
     rc = moc_launch_sweep(p);
     if (rc != MOC_OK) return fail(p, rc);
     if (cudaEventRecord(p->ev1, p->stream) != cudaSuccess) return fail(p, MOC_ERR_CUDA);
+    if (had_pending) {                 // the sweep applied the pending factor
+      p->psi_pending = false;
+      rc = moc_reset_psi_scale(p);
+      if (rc != MOC_OK) return fail(p, rc);
+    }
     if (cudaEventSynchronize(p->ev1) != cudaSuccess) return fail(p, MOC_ERR_CUDA);
     float ms = 0.f;
     cudaEventElapsedTime(&ms, p->ev0, p->ev1);
@@ -907,6 +952,7 @@ int moc_time_sweep(moc_problem *p, int iters, double *ms_per_sweep) {
 
 int moc_time_power_iterations(moc_problem *p, int iters, double *ms_total, double *ms_sweeps,
                               double *keff, double *residual) {
+  MOC_NVTX_RANGE("moc_time_power_iterations");
   int rc = ready(p);
   if (rc != MOC_OK) return rc;
   if (iters < 1) return MOC_ERR_ARG;
@@ -943,6 +989,60 @@ int moc_time_power_iterations(moc_problem *p, int iters, double *ms_total, doubl
   if (rc != MOC_OK) return fail(p, rc);
   if (ms_total) *ms_total = tot;
   if (ms_sweeps) *ms_sweeps = sweeps;
+  double sc[SC_COUNT];
+  rc = read_scalars(p, sc);
+  if (rc != MOC_OK) return rc;
+  if (keff) *keff = sc[SC_KEFF];
+  if (residual) *residual = sc[SC_RESIDUAL];
+  return MOC_OK;
+}
+
+int moc_time_phases(moc_problem *p, int iters, double *phase_ms, double *keff,
+                    double *residual) {
+  MOC_NVTX_RANGE("moc_time_phases");
+  int rc = ready(p);
+  if (rc != MOC_OK) return rc;
+  if (iters < 1 || !phase_ms) return MOC_ERR_ARG;
+  cudaSetDevice(p->device);
+  // per iteration: start, after the sweep, after renormalize, after update, after keff
+  constexpr int EV = 5;
+  std::vector<cudaEvent_t> ev((size_t)(EV * iters), nullptr);
+  for (auto &e : ev)
+    if (cudaEventCreate(&e) != cudaSuccess) {
+      for (auto &x : ev)
+        if (x) cudaEventDestroy(x);
+      return fail(p, MOC_ERR_CUDA);
+    }
+  for (int i = 0; i < iters && rc == MOC_OK; ++i) {
+    cudaEvent_t *e = ev.data() + (size_t)EV * i;
+    cudaEventRecord(e[0], p->stream);
+    rc = sweep_impl(p);
+    cudaEventRecord(e[1], p->stream);
+    if (rc == MOC_OK) rc = moc_launch_renormalize(p);
+    cudaEventRecord(e[2], p->stream);
+    // the reference's two calls, k_eff chained on the device (src/main.c:81,87)
+    if (rc == MOC_OK) rc = moc_launch_update(p, 0.0, true, false);
+    cudaEventRecord(e[3], p->stream);
+    if (rc == MOC_OK) rc = moc_launch_keff(p, 0.0);
+    cudaEventRecord(e[4], p->stream);
+  }
+  if (rc == MOC_OK && cudaEventSynchronize(ev.back()) != cudaSuccess) rc = MOC_ERR_CUDA;
+  double acc[MOC_N_PHASES] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  if (rc == MOC_OK) {
+    for (int i = 0; i < iters; ++i) {
+      const cudaEvent_t *e = ev.data() + (size_t)EV * i;
+      const int slot[4] = {MOC_PHASE_SWEEP, MOC_PHASE_RENORMALIZE, MOC_PHASE_UPDATE,
+                           MOC_PHASE_KEFF};
+      for (int k = 0; k < 4; ++k) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e[k], e[k + 1]);
+        acc[slot[k]] += ms;
+      }
+    }
+  }
+  for (auto &e : ev) cudaEventDestroy(e);
+  if (rc != MOC_OK) return fail(p, rc);
+  for (int k = 0; k < MOC_N_PHASES; ++k) phase_ms[k] = acc[k];   // no exchange on one device
   double sc[SC_COUNT];
   rc = read_scalars(p, sc);
   if (rc != MOC_OK) return rc;
@@ -1066,6 +1166,7 @@ int moc_fine_flux_storage(moc_problem *p, void **ptr, int64_t *n_elems, int32_t 
 // ---- adjoint ---------------------------------------------------------------
 
 int moc_adjoint_forward(moc_problem *p, int k_ckpt) {
+  MOC_NVTX_RANGE("moc_adjoint_forward");
   int rc = ready(p);
   if (rc != MOC_OK) return rc;
   if (k_ckpt < 1 || k_ckpt > 8) return MOC_ERR_ARG;
@@ -1094,6 +1195,7 @@ int moc_adjoint_forward(moc_problem *p, int k_ckpt) {
 
 int moc_adjoint_backward_fit(moc_problem *p, const float *dphi, float *dq, double *dsigt,
                              float *dpsi_in, float *dfit) {
+  MOC_NVTX_RANGE("moc_adjoint_backward");
   int rc = ready(p);
   if (rc != MOC_OK) return rc;
   if (!dphi || !p->ck_psi) return !dphi ? MOC_ERR_ARG : MOC_ERR_STATE;

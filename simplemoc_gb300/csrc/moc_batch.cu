@@ -362,6 +362,7 @@ int moc_batch_autotune(moc_batch *b) {
 }
 
 int moc_batch_sweep(moc_batch *b) {
+  MOC_NVTX_RANGE("moc_batch_sweep");
   if (!b) return MOC_ERR_ARG;
   cudaSetDevice(b->device);
   int rc = join_cores(b);
@@ -378,6 +379,7 @@ int moc_batch_sweep(moc_batch *b) {
 // one of them eagerly (kernel attributes get set and every core reaches the
 // pending renormalisation that the graph replays) and replays the rest.
 int moc_batch_power_iterations(moc_batch *b, int iters, int use_graph, double *ms_total) {
+  MOC_NVTX_RANGE("moc_batch_power_iterations");
   if (!b || iters < 1) return MOC_ERR_ARG;
   cudaSetDevice(b->device);
   int rc = join_cores(b);

@@ -11,6 +11,21 @@
 
 #include "moc_host.h"
 
+#include <nvtx3/nvToolsExt.h>
+
+// NVTX range over one entry point (header-only NVTX 3: a no-op unless a
+// profiler injects itself), so that a timeline shows the library's calls under
+// the reference's names.
+struct MocNvtxRange {
+  explicit MocNvtxRange(const char *name) { nvtxRangePushA(name); }
+  ~MocNvtxRange() { nvtxRangePop(); }
+  MocNvtxRange(const MocNvtxRange &) = delete;
+  MocNvtxRange &operator=(const MocNvtxRange &) = delete;
+};
+#define MOC_NVTX_CAT2(a, b) a##b
+#define MOC_NVTX_CAT(a, b) MOC_NVTX_CAT2(a, b)
+#define MOC_NVTX_RANGE(name) MocNvtxRange MOC_NVTX_CAT(moc_nvtx_range_, __LINE__)(name)
+
 // Coefficients per (sigma_t row, group): the interleaved planes of moc_host.h.
 enum { COEF_PLANES = MOC_COEF_PLANES };
 
@@ -27,6 +42,8 @@ struct SweepArgs {
   float *phi;               // [NS*F*ldg]
   float *phi_lo;            // [NS*F*ldg] compensation words (MIXED + flag) or null
   float *psi;               // [N3D*ldg]  forward angular flux, in place
+  float *rec;               // [N3D*S*ldg] recorded tallies (deterministic mode) or null
+  int32_t *rec_row;         // [N3D*S]     their FSR rows
   const float *psi_scale;   // pending renormalisation factor of psi, or null
   const double *q64;        // FP64 mode state
   double *phi64;
@@ -54,6 +71,8 @@ struct SweepArgs {
   const float *csr_z;       // [M] start heights
   const int32_t *csr_src;   // [M] source regions
 };
+
+struct MocDet;   // deterministic-order tally buffers (moc_determ.cu)
 
 struct moc_problem {
   moc_dims d;
@@ -132,6 +151,8 @@ struct moc_problem {
   void *h_stage = nullptr;                       // pinned host staging of derived arrays
   cudaEvent_t stage_ev = nullptr;                // after the last copy from h_stage
   bool stage_pending = false;
+  // deterministic-order tally mode: record / sort / ordered-add buffers
+  MocDet *det = nullptr;
   // host copies needed for re-upload and derived arrays
   float polar[64];
 };
@@ -153,6 +174,18 @@ int moc_shape_groups(int tpw, int cpl);
 int moc_launch_sweep(moc_problem *p);
 // The sweep of 2D tracks [i2_begin, i2_end) with all their 3D tracks.
 int moc_launch_sweep_range(moc_problem *p, int64_t i2_begin, int64_t i2_end);
+// The sweep of 2D tracks [i2_begin, i2_end) with recorded tallies (no flux
+// update): contribution of segment n of the range's track t at
+// rec[(t * S + n) * ldg], its FSR row at rec_row[t * S + n].
+int moc_launch_sweep_record(moc_problem *p, int64_t i2_begin, int64_t i2_end, float *rec,
+                            int32_t *rec_row);
+// Deterministic-order sweep (moc_determ.cu): the tallies of every FSR added in
+// the serial order of the tracks and their segments.
+int moc_det_sweep(moc_problem *p);
+void moc_det_release(moc_problem *p);
+// Device allocation counted against the handle's budget (moc_set_memory_limit).
+int moc_dev_alloc(moc_problem *p, void **ptr, int64_t bytes);
+void moc_dev_free(moc_problem *p, void *ptr, int64_t bytes);
 // Makes the stream wait for an upload in flight (no-op when there is none).
 int moc_join_upload(moc_problem *p);
 // Waits for the handle's stream and folds its device error word into the
@@ -206,6 +239,9 @@ int moc_set_leakage(moc_problem *p, double leakage);
 int moc_launch_keff(moc_problem *p, double leakage);
 int moc_post_scratch_blocks();
 int moc_psi_materialize(moc_problem *p);
+// FP64 mode with MOC_FLAG_FP32_STATE: rounds the chosen state arrays to FP32
+// values (no-op otherwise).
+int moc_round_state_fp32(moc_problem *p, bool flux, bool psi, bool source);
 int moc_detect_psi_b(moc_problem *p);
 
 // Scalars slots in p->scalars (double):

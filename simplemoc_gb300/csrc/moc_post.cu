@@ -580,10 +580,35 @@ int moc_detect_psi_b(moc_problem *p) {
   return MOC_OK;
 }
 
+__global__ void round_to_float_kernel(double *__restrict__ x, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    x[i] = (double)(float)x[i];
+}
+
+// MOC_FLAG_FP32_STATE: the FP64 state arrays rounded to FP32 values in place.
+int moc_round_state_fp32(moc_problem *p, bool flux, bool psi, bool source) {
+  if (p->mode != MOC_MODE_FP64 || !(p->flags & MOC_FLAG_FP32_STATE)) return MOC_OK;
+  int sms = 0;
+  MOC_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p->device));
+  const unsigned grid = (unsigned)(sms * 8);
+  if (flux) round_to_float_kernel<<<grid, 256, 0, p->stream>>>(p->phi64, p->nfsr * p->ldg);
+  if (source) round_to_float_kernel<<<grid, 256, 0, p->stream>>>(p->q64, p->nfsr * p->ldg);
+  if (psi) {
+    round_to_float_kernel<<<grid, 256, 0, p->stream>>>(p->psi_f64, p->n3d * p->ldg);
+    round_to_float_kernel<<<grid, 256, 0, p->stream>>>(p->psi_b64, p->n3d * p->ldg);
+  }
+  MOC_CUDA_TRY(cudaGetLastError());
+  p->launches += (flux ? 1 : 0) + (source ? 1 : 0) + (psi ? 2 : 0);
+  return MOC_OK;
+}
+
 int moc_launch_renormalize(moc_problem *p) {
-  if (p->mode == MOC_MODE_FP64)
-    return renorm_t<double>(p, p->phi64, p->psi_f64, p->psi_b64,
-                            reinterpret_cast<double *>(p->partials + 3 * RBLOCKS));
+  if (p->mode == MOC_MODE_FP64) {
+    const int rc = renorm_t<double>(p, p->phi64, p->psi_f64, p->psi_b64,
+                                    reinterpret_cast<double *>(p->partials + 3 * RBLOCKS));
+    return rc == MOC_OK ? moc_round_state_fp32(p, true, true, false) : rc;
+  }
   return renorm_t<float>(p, p->phi, p->psi_f, p->psi_b,
                          reinterpret_cast<float *>(p->partials + 3 * RBLOCKS));
 }
@@ -593,7 +618,10 @@ int moc_launch_update(moc_problem *p, double keff, bool keff_on_device, bool wit
     set_scalar<<<1, 1, 0, p->stream>>>(p->scalars, SC_KEFF_IN, keff);
     p->launches++;
   }
-  if (p->mode == MOC_MODE_FP64) return update_t<double>(p, p->phi64, p->q64, with_keff);
+  if (p->mode == MOC_MODE_FP64) {
+    const int rc = update_t<double>(p, p->phi64, p->q64, with_keff);
+    return rc == MOC_OK ? moc_round_state_fp32(p, false, false, true) : rc;
+  }
   return update_t<float>(p, p->phi, p->q, with_keff);
 }
 

@@ -559,6 +559,7 @@ int sweep_ref(int64_t *segments) {
 extern "C" {
 
 void transport_sweep(moc_ref_params *params, moc_ref_input *I) {
+  MOC_NVTX_RANGE("transport_sweep");
   std::lock_guard<std::mutex> lock(g_mu);
   if (!params || !I) {
     g_status = MOC_ERR_ARG;
@@ -579,6 +580,7 @@ void transport_sweep(moc_ref_params *params, moc_ref_input *I) {
 }
 
 void renormalize_flux(moc_ref_params params, moc_ref_input I, moc_ref_commgrid grid) {
+  MOC_NVTX_RANGE("renormalize_flux");
   (void)grid;
   std::lock_guard<std::mutex> lock(g_mu);
   int rc = ensure_state(&params, &I);
@@ -588,6 +590,7 @@ void renormalize_flux(moc_ref_params params, moc_ref_input I, moc_ref_commgrid g
 }
 
 float update_sources(moc_ref_params params, moc_ref_input I, float keff) {
+  MOC_NVTX_RANGE("update_sources");
   std::lock_guard<std::mutex> lock(g_mu);
   int rc = ensure_state(&params, &I);
   double res = NAN;
@@ -597,6 +600,7 @@ float update_sources(moc_ref_params params, moc_ref_input I, float keff) {
 }
 
 float compute_keff(moc_ref_params params, moc_ref_input I, moc_ref_commgrid grid) {
+  MOC_NVTX_RANGE("compute_keff");
   (void)grid;
   std::lock_guard<std::mutex> lock(g_mu);
   int rc = ensure_state(&params, &I);

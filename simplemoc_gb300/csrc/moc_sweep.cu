@@ -325,14 +325,35 @@ __device__ __forceinline__ float mixed_flat(float y, float sig, float r1, float 
   return w_mu * dpsi;
 }
 
-// Compensated tally: hi word by atomic add returning the old value, the
-// rounding error of that add (TwoSum) into the lo word.
-__device__ __forceinline__ void comp_add(float *hi, float *lo, float x) {
-  float old = atomicAdd(hi, x);
-  float s = old + x;
-  float bp = s - old;
-  float err = (old - (s - bp)) + (x - bp);
-  if (err != 0.0f) atomicAdd(lo, err);
+// The rounding error of old + x (TwoSum, Knuth): exact in round-to-nearest.
+__device__ __forceinline__ float two_sum_err(float old, float x) {
+  const float s = __fadd_rn(old, x);
+  const float bp = __fsub_rn(s, old);
+  return __fadd_rn(__fsub_rn(old, __fsub_rn(s, bp)), __fsub_rn(x, bp));
+}
+
+// A chunk of compensated tallies: one vector atomic that returns the old hi
+// words (atom.global.v4/.v2.f32, sm_90 and later), the TwoSum errors of the
+// chunk's additions, and one vector reduction of them into the lo words.  The
+// hi additions are the same single-rounding additions as the plain tallies;
+// the lo words collect what each of them rounded away.
+__device__ __forceinline__ void comp_add_vec(float *hi, float *lo, float4 t) {
+  float4 o;
+  asm volatile("atom.global.v4.f32.add {%0,%1,%2,%3}, [%4], {%5,%6,%7,%8};"
+               : "=f"(o.x), "=f"(o.y), "=f"(o.z), "=f"(o.w)
+               : "l"(hi), "f"(t.x), "f"(t.y), "f"(t.z), "f"(t.w)
+               : "memory");
+  red_add_v4(lo, two_sum_err(o.x, t.x), two_sum_err(o.y, t.y), two_sum_err(o.z, t.z),
+             two_sum_err(o.w, t.w));
+}
+__device__ __forceinline__ void comp_add_vec(float *hi, float *lo, float2 t) {
+  float2 o;
+  asm volatile("atom.global.v2.f32.add {%0,%1}, [%2], {%3,%4};"
+               : "=f"(o.x), "=f"(o.y)
+               : "l"(hi), "f"(t.x), "f"(t.y)
+               : "memory");
+  asm volatile("red.global.add.v2.f32 [%0], {%1,%2};" ::"l"(lo), "f"(two_sum_err(o.x, t.x)),
+               "f"(two_sum_err(o.y, t.y)));
 }
 
 // Loads of one segment that are issued one segment ahead (software pipeline):
@@ -377,7 +398,8 @@ __device__ __forceinline__ int checked_source(const SweepArgs &a, int s, int li)
 // One 3D track (or one group of TPW lanes' track) of the sweep.  TPW_CT is
 // the threads per track when known at compile time; 0 takes tpw_rt (the
 // batched kernel, where each core has its own width).
-template <int TPW_CT, int CPL, int MODE, bool QUAD, bool CSR, bool CKPT = false, int VW = 4>
+template <int TPW_CT, int CPL, int MODE, bool QUAD, bool CSR, bool CKPT = false, int VW = 4,
+          bool REC = false>
 __device__ __forceinline__ void sweep_track(const SweepArgs &a, int64_t track, int lane,
                                             int tpw_rt, const float2 *s_table) {
   const int TPW = TPW_CT ? TPW_CT : tpw_rt;
@@ -556,12 +578,19 @@ __device__ __forceinline__ void sweep_track(const SweepArgs &a, int64_t track, i
           set(psi[k], e, p);
         }
       }
-      if (valid) {
+      if (REC) {
+        // deterministic-order tallies: the contribution goes to the track's
+        // record slot (segment n of track tr), its FSR row beside it; an ordered
+        // reduction adds the records to the flux later
+        if (valid) {
+          const int64_t slot = tr * a.S + n;
+          *reinterpret_cast<V *>(a.rec + slot * a.ldg + g4) = t;
+          if (c == 0) a.rec_row[slot] = (int32_t)(g.frow / a.ldg);
+        }
+      } else if (valid) {
         float *dst = a.phi + g.frow + g4;
         if (MODE == MODE_MIXED && a.phi_lo != nullptr) {
-          float *lo = a.phi_lo + g.frow + g4;
-#pragma unroll
-          for (int e = 0; e < VW; ++e) comp_add(dst + e, lo + e, get(t, e));
+          comp_add_vec(dst, a.phi_lo + g.frow + g4, t);
         } else if (MODE == MODE_MIXED) {
           red_add_vec_last(dst, t, tally_pol);
         } else {
@@ -586,7 +615,7 @@ __device__ __forceinline__ void sweep_track(const SweepArgs &a, int64_t track, i
 // With TPW not dividing 32 the last 32 % TPW lanes own no track: they run the
 // loop on an out-of-range track (loads clamped to a real one, no stores) so that
 // the warp's shuffles stay converged.
-template <int TPW, int CPL, int MODE, bool QUAD, bool CSR, bool CKPT, int VW>
+template <int TPW, int CPL, int MODE, bool QUAD, bool CSR, bool CKPT, int VW, bool REC = false>
 __device__ __forceinline__ void sweep_body(const SweepArgs &a, float2 *s_table) {
   if (MODE == MODE_PLAIN) {
     for (int i = threadIdx.x; i < a.table_n; i += BLOCK) s_table[i] = a.table[i];
@@ -598,14 +627,22 @@ __device__ __forceinline__ void sweep_body(const SweepArgs &a, float2 *s_table) 
   const int64_t warp_id = ((int64_t)blockIdx.x * BLOCK + threadIdx.x) >> 5;
   const int64_t n_warps = ((int64_t)gridDim.x * BLOCK) >> 5;
   for (int64_t base = warp_id * GPW; base < a.n3d; base += n_warps * GPW)
-    sweep_track<TPW, CPL, MODE, QUAD, CSR, CKPT, VW>(a, gw < GPW ? base + gw : a.n3d, lane,
-                                                     TPW, s_table);
+    sweep_track<TPW, CPL, MODE, QUAD, CSR, CKPT, VW, REC>(a, gw < GPW ? base + gw : a.n3d, lane,
+                                                          TPW, s_table);
 }
 
 template <int TPW, int CPL, int MODE, bool QUAD, bool CSR = false, bool CKPT = false>
 __global__ void __launch_bounds__(BLOCK) sweep_kernel(SweepArgs a) {
   extern __shared__ float2 s_table[];
   sweep_body<TPW, CPL, MODE, QUAD, CSR, CKPT, 4>(a, s_table);
+}
+
+// The sweep with recorded tallies (deterministic-order mode): every segment's
+// contribution is stored, not added.
+template <int TPW, int CPL, int MODE, bool QUAD>
+__global__ void __launch_bounds__(BLOCK) sweep_record_kernel(SweepArgs a) {
+  extern __shared__ float2 s_table[];
+  sweep_body<TPW, CPL, MODE, QUAD, false, false, 4, true>(a, s_table);
 }
 
 // Two-group chunks: held to two blocks an SM (the MIXED quadratic variant
@@ -863,11 +900,7 @@ __global__ void __launch_bounds__(BLOCK) sweep_staged_kernel(SweepArgs a, int ro
         if (valid) {
           float *dst = a.phi + sg.frow + g4;
           if (MODE == MODE_MIXED && a.phi_lo != nullptr) {
-            float *lo = a.phi_lo + sg.frow + g4;
-            comp_add(dst + 0, lo + 0, t.x);
-            comp_add(dst + 1, lo + 1, t.y);
-            comp_add(dst + 2, lo + 2, t.z);
-            comp_add(dst + 3, lo + 3, t.w);
+            comp_add_vec(dst, a.phi_lo + sg.frow + g4, t);
           } else {
             red_add_v4(dst, t.x, t.y, t.z, t.w);
           }
@@ -971,27 +1004,32 @@ __global__ void __launch_bounds__(BLOCK) sweep64_kernel(SweepArgs a) {
       const double *qr = a.q64 + (sb + r0) * a.ldg;
       double *fr = a.phi64 + (sb + fine) * a.ldg;
       const float *sigr = a.coef + (int64_t)__ldg(a.src_sigt + s) * COEF_PLANES * a.ldg;
+      // one FP64 division per (segment, group): the divisors of src/solver.c
+      // (sigma^k, 2dz, 2dz^2) become products with reciprocals, a change of a
+      // few units in the 16th digit (the FP64 pipe is the yardstick's bound)
+      const double r2dz = 1.0 / (2.0 * dz), r2dz2 = 1.0 / (2.0 * dz * dz);
       for (int g = li; g < a.G; g += TPW) {
         const double sig = sigr[(g >> 2) * 4 * COEF_PLANES + (g & 3)];
+        const double rs = 1.0 / sig;
         const double tau = sig * ds;
         const double e = -expm1(-tau);
         double p = a.psi64[tr * a.ldg + g];
         double tally;
         if (QUAD) {
           const double y1 = qr[g], y2 = qr[a.ldg + g], y3 = qr[2 * a.ldg + g];
-          const double c1 = (y1 - y3) / (2.0 * dz);
-          const double c2 = (y1 - 2.0 * y2 + y3) / (2.0 * dz * dz);
+          const double c1 = (y1 - y3) * r2dz;
+          const double c2 = (y1 - 2.0 * y2 + y3) * r2dz2;
           const double q0 = y2 + c1 * zin + c2 * zin * zin;
           const double q1 = c1 + 2.0 * c2 * zin;
-          const double sig2 = sig * sig;
-          const double reuse = tau * (tau - 2.0) + 2.0 * e / (sig * sig2);
-          const double fi = (q0 * tau + (sig * p - q0) * e) / sig2 + q1 * mu * reuse +
-                            c2 * mu2 * (tau * (tau * (tau - 3.0) + 6.0) - 6.0 * e) /
-                                (3.0 * sig2 * sig2);
+          const double rs2 = rs * rs;
+          const double reuse = tau * (tau - 2.0) + 2.0 * e * (rs * rs2);
+          const double fi = (q0 * tau + (sig * p - q0) * e) * rs2 + q1 * mu * reuse +
+                            c2 * mu2 * (tau * (tau * (tau - 3.0) + 6.0) - 6.0 * e) *
+                                (rs2 * rs2 * (1.0 / 3.0));
           tally = w * fi;
-          p = q0 * e / sig + q1 * mu * (tau - e) / sig2 + c2 * mu2 * reuse + p * (1.0 - e);
+          p = q0 * e * rs + q1 * mu * (tau - e) * rs2 + c2 * mu2 * reuse + p * (1.0 - e);
         } else {
-          const double dpsi = (p - qr[g] / sig) * e;
+          const double dpsi = (p - qr[g] * rs) * e;
           p -= dpsi;
           tally = w * mu * dpsi;
         }
@@ -1006,10 +1044,12 @@ __global__ void __launch_bounds__(BLOCK) sweep64_kernel(SweepArgs a) {
 }
 
 template <int TPW, int CPL, int MODE, bool QUAD, bool CSR = false, bool CKPT = false,
-          int VW = 4>
+          int VW = 4, bool REC = false>
 int launch_t(moc_problem *p, const SweepArgs &a) {
   void (*kern)(SweepArgs);
-  if constexpr (VW == 4)
+  if constexpr (REC)
+    kern = sweep_record_kernel<TPW, CPL, MODE, QUAD>;
+  else if constexpr (VW == 4)
     kern = sweep_kernel<TPW, CPL, MODE, QUAD, CSR, CKPT>;
   else
     kern = sweep_kernel_v2<TPW, CPL, MODE, QUAD, CSR, CKPT>;
@@ -1242,6 +1282,41 @@ int moc_launch_sweep_range(moc_problem *p, int64_t i2_begin, int64_t i2_end) {
   a.psi += t0 * p->ldg;
   a.n3d = (i2_end - i2_begin) * P * Z;
   return launch_args(p, a, tpw, cpl, p->stages > 0 ? p->stages : 0);
+}
+
+namespace {
+template <int MODE, bool QUAD>
+int dispatch_record(moc_problem *p, const SweepArgs &a) {
+  if (p->ldg <= 128) return launch_t<16, 2, MODE, QUAD, false, false, 4, true>(p, a);
+  if (p->ldg <= 256) return launch_t<32, 2, MODE, QUAD, false, false, 4, true>(p, a);
+  return MOC_ERR_UNSUPPORTED;
+}
+}  // namespace
+
+// The sweep of 2D tracks [i2_begin, i2_end) with its tallies recorded: the
+// contribution of segment n of the range's track t (counted from the range's
+// first track) goes to rec[(t * S + n) * ldg ...], its FSR row to
+// rec_row[t * S + n].
+int moc_launch_sweep_record(moc_problem *p, int64_t i2_begin, int64_t i2_end, float *rec,
+                            int32_t *rec_row) {
+  const int64_t P = p->d.n_polar, Z = p->d.z_stacked, S = p->d.n_seg;
+  if (i2_begin < 0 || i2_end > p->d.n_tracks_2d || i2_begin >= i2_end) return MOC_ERR_ARG;
+  if (p->mode == MOC_MODE_FP64) return MOC_ERR_UNSUPPORTED;
+  SweepArgs a = build_args(p);
+  const int64_t t0 = i2_begin * P * Z;
+  a.seg_ds += i2_begin * P * S;
+  a.seg_src += t0 * S;
+  a.weight += t0;
+  a.z0 += t0;
+  a.psi += t0 * p->ldg;
+  a.n3d = (i2_end - i2_begin) * P * Z;
+  a.phi_lo = nullptr;
+  a.rec = rec;
+  a.rec_row = rec_row;
+  const bool quad = p->d.axial_exp == 2;
+  if (p->mode == MOC_MODE_PLAIN)
+    return quad ? dispatch_record<MODE_PLAIN, true>(p, a) : dispatch_record<MODE_PLAIN, false>(p, a);
+  return quad ? dispatch_record<MODE_MIXED, true>(p, a) : dispatch_record<MODE_MIXED, false>(p, a);
 }
 
 // Times every launch shape that covers the groups on the first n_sub tracks.

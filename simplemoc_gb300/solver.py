@@ -25,7 +25,8 @@ MODES = {"plain": L.MOC_MODE_PLAIN, "mixed": L.MOC_MODE_MIXED, "fp64": L.MOC_MOD
 
 class Solver:
     def __init__(self, problem: HostProblem, device: int = 0, mode: str = "plain",
-                 compensated: bool = False, simt_update: bool = False):
+                 compensated: bool = False, simt_update: bool = False,
+                 deterministic: bool = False, fp32_state: bool = False):
         self._lib = L._lib()
         self.problem = problem
         self.spec = problem.spec
@@ -36,7 +37,7 @@ class Solver:
                                      C.byref(h)), "moc_create")
         self._h = h
         self.mode = "plain"
-        self.set_mode(mode, compensated, simt_update)
+        self.set_mode(mode, compensated, simt_update, deterministic, fp32_state)
 
     # ---- lifecycle ---------------------------------------------------------
     def close(self) -> None:
@@ -60,12 +61,17 @@ class Solver:
     def handle(self) -> C.c_void_p:
         return self._h
 
-    def set_mode(self, mode: str, compensated: bool = False, simt_update: bool = False) -> None:
+    def set_mode(self, mode: str, compensated: bool = False, simt_update: bool = False,
+                 deterministic: bool = False, fp32_state: bool = False) -> None:
         """mode: "plain", "mixed" or "fp64".  compensated: MIXED tallies with
         compensation.  simt_update: MIXED update_sources on the CUDA cores
-        instead of the tensor cores."""
+        instead of the tensor cores.  deterministic: tallies added in the
+        serial order of tracks and segments (PLAIN, MIXED).  fp32_state: FP64
+        arithmetic on state rounded to FP32 values (the FP32-storage floor)."""
         flags = (L.MOC_FLAG_COMPENSATED if compensated else 0) | \
-            (L.MOC_FLAG_SIMT_UPDATE if simt_update else 0)
+            (L.MOC_FLAG_SIMT_UPDATE if simt_update else 0) | \
+            (L.MOC_FLAG_DETERMINISTIC if deterministic else 0) | \
+            (L.MOC_FLAG_FP32_STATE if fp32_state else 0)
         L.check(self._lib.moc_set_mode(self._h, MODES[mode], flags), "moc_set_mode")
         self.mode = mode
 
@@ -158,6 +164,17 @@ class Solver:
                 "time_power_iterations")
         return {"ms_total": tot.value, "ms_sweeps": sw.value, "keff": k.value,
                 "residual": r.value}
+
+    def time_phases(self, iters: int) -> dict:
+        """Device time of each phase of `iters` power iterations, under the
+        reference's phase names (src/main.c:103-113), in milliseconds summed
+        over the iterations, plus the final k_eff and residual."""
+        ms = (C.c_double * len(L.PHASE_NAMES))()
+        k, r = C.c_double(), C.c_double()
+        L.check(self._lib.moc_time_phases(self._h, iters, ms, C.byref(k), C.byref(r)),
+                "moc_time_phases")
+        return {"phases_ms": dict(zip(L.PHASE_NAMES, (float(x) for x in ms))),
+                "keff": k.value, "residual": r.value}
 
     def launch_count(self) -> int:
         return int(self._lib.moc_launch_count(self._h))
