@@ -456,11 +456,13 @@ def run_dropin(args):
     include/simplemoc_refabi.h) on a reference-layout problem of the small
     problem's size: 1024 2D tracks of ~50 segments, 4 polar angles, 300 stacked
     rays over 200 cm, 100 groups.  The traversal is the reference's (axial
-    splitting, stacked-ray retirement) in PLAIN arithmetic; source ids come from
-    the counter hash (the libc rand() sequence is drawn on the host, for parity
-    runs).  A step is one power iteration through the four symbols (each returns
-    on the host, as the reference's do); integrations = the traversal's 3D
-    sub-segments x groups."""
+    splitting, stacked-ray retirement) in PLAIN arithmetic.  A step is one power
+    iteration through the four symbols (each returns on the host, as the
+    reference's do); integrations = the traversal's 3D sub-segments x groups.
+    The value is the library's default source-id mode, libc rand() drawn on the
+    host in the serial reference's order (what an unchanged src/main.c gets);
+    the counter-hash mode, whose ids are drawn on the device, is reported
+    beside it."""
     import ctypes as C
 
     import simplemoc_gb300 as sm
@@ -470,39 +472,50 @@ def run_dropin(args):
     Z = spec.z_stacked
     geo = refabi.make_geometry(spec.seed + 1, spec.n_tracks_2d, spec.n_polar, Z, 50.0,
                                spec.height / Z)
-    rp = refabi.build(hp, geo)
-    lb = refabi.lib()
-    lb.moc_ref_finalize()
-    lb.moc_ref_set_rng(refabi.RNG_HASH, 1234)
-    grid = refabi.CommGrid()
-    keff = [1.0]
-
-    def step():
-        lb.transport_sweep(C.byref(rp.params), C.byref(rp.input))
-        lb.renormalize_flux(rp.params, rp.input, grid)
-        lb.update_sources(rp.params, rp.input, keff[0])
-        keff[0] = lb.compute_keff(rp.params, rp.input, grid)
-        if lb.moc_ref_status() != 0:
-            raise RuntimeError(f"drop-in status {lb.moc_ref_status()}")
-        return int(lb.moc_ref_last_segments())
-
-    K, W = max(1, args.steps), max(1, args.warmup)
-    for _ in range(W):
-        step()
-    t0 = time.perf_counter()
-    segs = sum(step() for _ in range(K))
-    dt = time.perf_counter() - t0
-    lb.moc_ref_finalize()
     G = spec.n_groups
+    K, W = max(1, args.steps), max(1, args.warmup)
+    lb = refabi.lib()
+    out = {}
+    for mode_name, mode in (("hash", refabi.RNG_HASH), ("libc", refabi.RNG_LIBC)):
+        rp = refabi.build(hp, geo)
+        lb.moc_ref_finalize()
+        lb.moc_ref_set_rng(mode, 1234)
+        grid = refabi.CommGrid()
+        keff = [1.0]
+        rng_ms = []
+
+        def step():
+            lb.transport_sweep(C.byref(rp.params), C.byref(rp.input))
+            rng_ms.append(float(lb.moc_ref_last_rng_ms()))
+            lb.renormalize_flux(rp.params, rp.input, grid)
+            lb.update_sources(rp.params, rp.input, keff[0])
+            keff[0] = lb.compute_keff(rp.params, rp.input, grid)
+            if lb.moc_ref_status() != 0:
+                raise RuntimeError(f"drop-in status {lb.moc_ref_status()}")
+            return int(lb.moc_ref_last_segments())
+
+        for _ in range(W):
+            step()
+        rng_ms.clear()
+        t0 = time.perf_counter()
+        segs = sum(step() for _ in range(K))
+        dt = time.perf_counter() - t0
+        lb.moc_ref_finalize()
+        out[mode_name] = {"value": segs * G / dt, "ms_per_step": 1e3 * dt / K,
+                          "rng_ms_per_step": float(np.mean(rng_ms)),
+                          "sub_segments_per_sweep": segs // K, "keff": keff[0]}
     line = {
         "metric": "segment-group integrations/s per power iteration through the reference's "
-                  "entry points", "value": segs * G / dt, "unit": "integrations/s",
-        "n_gpus": 1, "steps": K, "warmup": W, "ms_per_step": 1e3 * dt / K,
+                  "entry points", "value": out["libc"]["value"], "unit": "integrations/s",
+        "n_gpus": 1, "steps": K, "warmup": W, "ms_per_step": out["libc"]["ms_per_step"],
         "higher_is_better": True, "dtype": "f32", "data": "synthetic (seeded)",
         "config": {"workload": f"drop-in: {spec.n_tracks_2d} 2D tracks x {spec.n_polar} polar x "
                                f"{Z} stacked rays, {G} groups, reference traversal, PLAIN",
-                   "sub_segments_per_sweep": segs // K},
-        "keff": keff[0],
+                   "source_ids": "libc rand() on the host, the serial reference's sequence",
+                   "sub_segments_per_sweep": out["libc"]["sub_segments_per_sweep"]},
+        "libc_rand_ms_per_step": out["libc"]["rng_ms_per_step"],
+        "hash": {k: out["hash"][k] for k in ("value", "ms_per_step", "sub_segments_per_sweep")},
+        "keff": out["libc"]["keff"],
     }
     print(json.dumps(line), flush=True)
 

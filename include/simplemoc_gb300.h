@@ -345,6 +345,24 @@ int moc_adjoint_backward(moc_problem *p, const float *dphi, float *dq, double *d
  * summed over those segments.  Quadratic source only (MOC_ERR_UNSUPPORTED). */
 int moc_adjoint_backward_fit(moc_problem *p, const float *dphi, float *dq, double *dsigt,
                              float *dpsi_in, float *dfit);
+/* Reverse mode of update_sources (src/solver.c:1235-1300) for the adjoint
+ * workload, whose source is one update step from a scalar flux phi0:
+ *   q[r][g] = (chi[m][g] * sum_h nuSigmaF[m][h] phi0[r][h] / k
+ *              + sum_h S[m][g][h] phi0[r][h]) / (4 pi)
+ * for each fine region r of a source of material m.  Given dL/dq it writes
+ * (device arrays; NULL skips):
+ *   dscatter [n_xs*G*G]  dL/dS, FP64 (row g = destination group)
+ *   dnusf    [n_xs*G]    dL/dnuSigmaF through the fission source, FP64
+ *   dphi0    [NS*F*G]    dL/dphi0
+ * phi0 and dq are [NS*F*G] (row stride G).  Up to 256 groups. */
+int moc_update_sources_adjoint(moc_problem *p, const float *phi0, const float *dq, double keff,
+                               double *dscatter, double *dnusf, float *dphi0);
+/* Replaces the cross-section tables (host arrays [n_xs*G*3] and [n_xs*G*G],
+ * the layout of moc_host) and everything derived from them. */
+int moc_set_cross_sections(moc_problem *p, const float *xs, const float *scatter);
+/* The scalar flux from / the fine source to device arrays (row stride G). */
+int moc_set_fine_flux_device(moc_problem *p, const float *phi);
+int moc_get_fine_source_device(moc_problem *p, float *q);
 /* Lanes per track (1..32, any width) and 4-group chunks per lane (1 or 2) of
  * the reverse sweep; 0, 0 = automatic (ceil(G/4) lanes of one chunk up to 128
  * groups).  MOC_ERR_ARG when lanes x chunks x 4 < G. */

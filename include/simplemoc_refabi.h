@@ -157,6 +157,10 @@ void moc_ref_finalize(void);
 int moc_ref_status(void);
 /* Sub-segments of the last sweep (Input.segments_processed). */
 int64_t moc_ref_last_segments(void);
+/* Host milliseconds the last sweep spent drawing its rand() values
+ * (MOC_REF_RNG_LIBC: one libc rand() per sub-segment on the calling thread,
+ * the serial reference's sequence; 0 in the hash mode). */
+double moc_ref_last_rng_ms(void);
 
 #ifdef __cplusplus
 }

@@ -122,6 +122,11 @@ SIGNATURES = {
     "moc_adjoint_backward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                        C.c_void_p]),
     "moc_set_adjoint_width": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "moc_update_sources_adjoint": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double,
+                                             C.c_void_p, C.c_void_p, C.c_void_p]),
+    "moc_set_cross_sections": (C.c_int, [C.c_void_p, f32p, f32p]),
+    "moc_set_fine_flux_device": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "moc_get_fine_source_device": (C.c_int, [C.c_void_p, C.c_void_p]),
     "moc_set_memory_limit": (C.c_int, [C.c_int64]),
     "moc_inject_fault": (C.c_int, [C.c_void_p, C.c_int]),
     "moc_selftest_wait": (C.c_int, [C.c_void_p, C.c_int64]),

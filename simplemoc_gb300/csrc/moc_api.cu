@@ -8,6 +8,7 @@
 #include <string.h>
 
 #include <atomic>
+#include <cmath>
 #include <new>
 #include <vector>
 
@@ -134,6 +135,27 @@ int put(moc_problem *p, T *dst, const T *src, int64_t count, cudaStream_t st = n
     int rc_ = (x);                  \
     if (rc_ != MOC_OK) return rc_;  \
   } while (0)
+
+// Per material the tensor-core update's second operand: rows n < G the
+// scatter rows S[m][n][.], n = G nuSigmaF, n = G + 1 SigmaA, split into TF32
+// hi and lo planes in the canonical K-major layout.
+void build_tc_b(const moc_problem *p, const float *xs, const float *scatter, float *tc_b) {
+  const moc_dims &d = p->d;
+  const int64_t G = d.n_groups;
+  const int np = p->tc_np;
+  const int64_t plane = (int64_t)np * p->tc_kp;
+  std::memset(tc_b, 0, sizeof(float) * (size_t)(d.n_xs * 2 * plane));
+  for (int64_t m = 0; m < d.n_xs; ++m)
+    for (int n = 0; n < G + 2; ++n)
+      for (int k = 0; k < G; ++k) {
+        const float v = n < G ? scatter[(m * G + n) * G + k]            // S[m][to n][from k]
+                              : xs[(m * G + k) * 3 + (n - G)];          // nuSigmaF, SigmaA
+        const float hi = moc_tf32_rna(v);
+        const int64_t o = m * 2 * plane + moc_tc_b_offset(n, k, np);
+        tc_b[(size_t)o] = hi;
+        tc_b[(size_t)(o + plane)] = moc_tf32_rna(v - hi);
+      }
+}
 
 // Host staging of the arrays the upload derives: one pinned block per handle,
 // allocated on the first upload, so that their copies are asynchronous (a copy
@@ -283,23 +305,11 @@ int upload_all(moc_problem *p, const moc_host *h, bool stream_tracks) {
           tc_items[n_tc++] = (int32_t)a;
           tc_items[n_tc++] = (int32_t)b;
         }
-      const int kp = p->tc_kp, np = p->tc_np;
-      const int64_t plane = (int64_t)np * kp;
-      float *tc_b = sg.tc_b;
-      std::memset(tc_b, 0, sizeof(float) * (size_t)(d.n_xs * 2 * plane));
-      for (int64_t m = 0; m < d.n_xs; ++m)
-        for (int n = 0; n < G + 2; ++n)
-          for (int k = 0; k < G; ++k) {
-            const float v = n < G ? h->scatter[(m * G + n) * G + k]            // S[m][to n][from k]
-                                  : h->xs[(m * G + k) * 3 + (n - G)];          // nuSigmaF, SigmaA
-            const float hi = moc_tf32_rna(v);
-            const int64_t o = m * 2 * plane + moc_tc_b_offset(n, k, np);
-            tc_b[(size_t)o] = hi;
-            tc_b[(size_t)(o + plane)] = moc_tf32_rna(v - hi);
-          }
+      const int64_t plane = (int64_t)p->tc_np * p->tc_kp;
+      build_tc_b(p, h->xs, h->scatter, sg.tc_b);
       p->n_tc_items = (int32_t)(n_tc / 3);
       TRY(put(p, p->tc_items, tc_items, n_tc));
-      TRY(put(p, p->tc_b, tc_b, d.n_xs * 2 * plane));
+      TRY(put(p, p->tc_b, sg.tc_b, d.n_xs * 2 * plane));
     }
     // the staged sources are reused by the next upload once these copies ran
     MOC_CUDA_TRY(cudaEventRecord(p->stage_ev, p->stream));
@@ -1101,6 +1111,72 @@ int moc_set_sigma_t(moc_problem *p, const float *sigt) {
   moc_host_coef(&p->d, sigt, p->ldg, coef.data());
   rc = put(p, p->coef, coef.data(), (int64_t)coef.size());
   if (rc == MOC_OK && cudaStreamSynchronize(p->stream) != cudaSuccess) rc = MOC_ERR_CUDA;
+  return rc == MOC_OK ? MOC_OK : fail(p, rc);
+}
+
+int moc_set_cross_sections(moc_problem *p, const float *xs, const float *scatter) {
+  int rc = ready(p);
+  if (rc != MOC_OK) return rc;
+  if (!xs || !scatter) return MOC_ERR_ARG;
+  const moc_dims &d = p->d;
+  const int64_t G = d.n_groups, nx = d.n_xs;
+  for (int64_t k = 0; k < nx * G * 3; ++k)
+    if (!std::isfinite(xs[k])) return MOC_ERR_ARG;
+  for (int64_t k = 0; k < nx * G * G; ++k)
+    if (!std::isfinite(scatter[k])) return MOC_ERR_ARG;
+  cudaSetDevice(p->device);
+  // the update kernel reads the scatter matrix transposed: St[m][from][to]
+  std::vector<float> st((size_t)(nx * G * G));
+  for (int64_t m = 0; m < nx; ++m)
+    for (int64_t g = 0; g < G; ++g)
+      for (int64_t h = 0; h < G; ++h) st[(size_t)((m * G + h) * G + g)] = scatter[(m * G + g) * G + h];
+  rc = put(p, p->xs, xs, nx * G * 3);
+  if (rc == MOC_OK) rc = put(p, p->scatter_t, st.data(), nx * G * G);
+  std::vector<float> tcb;
+  if (rc == MOC_OK && p->tc_b) {
+    tcb.resize((size_t)(nx * 2 * p->tc_np * p->tc_kp));
+    build_tc_b(p, xs, scatter, tcb.data());
+    rc = put(p, p->tc_b, tcb.data(), (int64_t)tcb.size());
+  }
+  if (rc == MOC_OK && cudaStreamSynchronize(p->stream) != cudaSuccess) rc = MOC_ERR_CUDA;
+  return rc == MOC_OK ? MOC_OK : fail(p, rc);
+}
+
+int moc_set_fine_flux_device(moc_problem *p, const float *phi) {
+  int rc = ready(p);
+  if (rc != MOC_OK) return rc;
+  if (!phi) return MOC_ERR_ARG;
+  cudaSetDevice(p->device);
+  const int64_t G = p->d.n_groups;
+  rc = copy_rows_dd(p, p->phi, p->ldg, phi, G, p->nfsr, G);
+  if (rc == MOC_OK && p->phi_lo)
+    rc = cudaMemsetAsync(p->phi_lo, 0, sizeof(float) * (size_t)(p->nfsr * p->ldg), p->stream) ==
+                 cudaSuccess ? MOC_OK : MOC_ERR_CUDA;
+  if (rc == MOC_OK && p->phi64) {
+    widen_kernel<<<1024, 256, 0, p->stream>>>(p->phi, p->phi64, p->nfsr * p->ldg);
+    p->launches++;
+  }
+  return rc == MOC_OK ? MOC_OK : fail(p, rc);
+}
+
+int moc_get_fine_source_device(moc_problem *p, float *q) {
+  int rc = ready(p);
+  if (rc != MOC_OK) return rc;
+  if (!q) return MOC_ERR_ARG;
+  cudaSetDevice(p->device);
+  rc = copy_rows_dd(p, q, (int64_t)p->d.n_groups, p->q, p->ldg, p->nfsr, p->d.n_groups);
+  return rc == MOC_OK ? MOC_OK : fail(p, rc);
+}
+
+int moc_update_sources_adjoint(moc_problem *p, const float *phi0, const float *dq, double keff,
+                               double *dscatter, double *dnusf, float *dphi0) {
+  MOC_NVTX_RANGE("update_sources_adjoint");
+  int rc = ready(p);
+  if (rc != MOC_OK) return rc;
+  if (!phi0 || !dq || !(keff != 0.0)) return MOC_ERR_ARG;
+  if (p->d.n_groups > 256) return MOC_ERR_UNSUPPORTED;
+  cudaSetDevice(p->device);
+  rc = moc_launch_update_adjoint(p, phi0, dq, keff, dscatter, dnusf, dphi0);
   return rc == MOC_OK ? MOC_OK : fail(p, rc);
 }
 

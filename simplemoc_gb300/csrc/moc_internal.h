@@ -239,6 +239,9 @@ int moc_set_leakage(moc_problem *p, double leakage);
 int moc_launch_keff(moc_problem *p, double leakage);
 int moc_post_scratch_blocks();
 int moc_psi_materialize(moc_problem *p);
+// Adjoint of update_sources (moc_update_adj.cu): device arrays, row stride G.
+int moc_launch_update_adjoint(moc_problem *p, const float *phi0, const float *dq, double keff,
+                              double *dscatter, double *dnusf, float *dphi0);
 // FP64 mode with MOC_FLAG_FP32_STATE: rounds the chosen state arrays to FP32
 // values (no-op otherwise).
 int moc_round_state_fp32(moc_problem *p, bool flux, bool psi, bool source);

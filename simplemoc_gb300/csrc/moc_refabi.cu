@@ -23,6 +23,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <chrono>
 #include <map>
 #include <mutex>
 #include <utility>
@@ -100,12 +101,61 @@ __device__ __forceinline__ int32_t sub_segment_source(const RefArgs &r, int64_t 
                               (uint64_t)r.ns, r.ns_m);
 }
 
+// Staged stores of the emitting pass.  Each lane writes the sub-segments of a
+// different stacked ray, so direct 4-byte stores scatter over as many sectors
+// as lanes; partly written sectors then cost a read and a write each in DRAM.
+// Instead each ray's entries collect in an 8-entry group in shared memory
+// (ds, z, source: 24 words) and leave as whole 32-byte sectors of each stream
+// once the group is full.  A ray's first and last groups are shared with the
+// neighbouring rays' streams and go out entry by entry.
+// Writes the entries [max(g0, first), end) of the group that ends at `end`
+// (g0 = the group's first slot, a multiple of 8).
+__device__ __forceinline__ void stage_flush(const RefArgs &r, const float *buf, int64_t first,
+                                            int64_t end) {
+  const int64_t g0 = (end - 1) & ~int64_t(7);
+  const int32_t *bsrc = reinterpret_cast<const int32_t *>(buf + 16);
+  if (g0 >= first && end - g0 == 8) {
+    // whole group: the streams are 256-byte aligned, so slot g0 starts a sector
+    float4 *ds4 = reinterpret_cast<float4 *>(r.sds + g0);
+    float4 *z4 = reinterpret_cast<float4 *>(r.sz + g0);
+    int4 *s4 = reinterpret_cast<int4 *>(r.ssrc + g0);
+    ds4[0] = make_float4(buf[0], buf[1], buf[2], buf[3]);
+    ds4[1] = make_float4(buf[4], buf[5], buf[6], buf[7]);
+    z4[0] = make_float4(buf[8], buf[9], buf[10], buf[11]);
+    z4[1] = make_float4(buf[12], buf[13], buf[14], buf[15]);
+    s4[0] = make_int4(bsrc[0], bsrc[1], bsrc[2], bsrc[3]);
+    s4[1] = make_int4(bsrc[4], bsrc[5], bsrc[6], bsrc[7]);
+    return;
+  }
+  for (int64_t x = g0 > first ? g0 : first; x < end; ++x) {
+    const int e = (int)(x - g0);
+    r.sds[x] = buf[e];
+    r.sz[x] = buf[8 + e];
+    r.ssrc[x] = bsrc[e];
+  }
+}
+
+// One entry of a ray's stream at slot x: into its group, which goes out when
+// its last entry arrives.
+__device__ __forceinline__ void stage_put(const RefArgs &r, float *buf, int64_t first, int64_t x,
+                                          float ds, float zh, int32_t src) {
+  const int e = (int)(x & 7);
+  buf[e] = ds;
+  buf[8 + e] = zh;
+  reinterpret_cast<int32_t *>(buf + 16)[e] = src;
+  if (e == 7) stage_flush(r, buf, first, x + 1);
+}
+
 // One 3D track over one 2D segment: the while loop of src/solver.c:409-524.
 // Returns the number of sub-segments; *hit = the track reached a domain bound
 // (and was reset); zh is updated by the reference's rule (src/solver.c:514-523).
+// EMIT: the sub-segments go to slots slot, slot + 1, ... of the streams, through
+// the ray's staging group `stg` (the ray's stream starts at slot `first`) or,
+// with stg null, directly.
 template <bool EMIT>
 __device__ int track_segment(const RefArgs &r, bool pos, double cos_d, float s_full, float &zh,
-                             bool last_seg, int k, bool *hit, int64_t slot, int64_t seq) {
+                             bool last_seg, int k, bool *hit, int64_t slot, int64_t seq,
+                             float *stg = nullptr, int64_t first = 0) {
   float s = s_full;
   // get_pos_interval / get_neg_interval (src/solver.c:895-907): float z / dz
   int curr = pos ? __float2int_rz(__fdiv_rn(zh, r.fine_dz_f))
@@ -140,9 +190,14 @@ __device__ int track_segment(const RefArgs &r, bool pos, double cos_d, float s_f
       }
     }
     if (EMIT) {
-      r.sds[slot + count] = ds;
-      r.sz[slot + count] = zh;
-      r.ssrc[slot + count] = sub_segment_source(r, seq + count);
+      const int32_t src = sub_segment_source(r, seq + count);
+      if (stg) {
+        stage_put(r, stg, first, slot + count, ds, zh, src);
+      } else {
+        r.sds[slot + count] = ds;
+        r.sz[slot + count] = zh;
+        r.ssrc[slot + count] = src;
+      }
     }
     ++count;
     if (last_seg || reset)
@@ -162,9 +217,13 @@ __device__ __forceinline__ int warp_incl_scan(int v, int lane) {
   return v;
 }
 
-template <int PASS>
+// STAGED (pass 1): the warp's stacked rays keep their staging groups in
+// dynamic shared memory, 24 words per ray, Z rays per warp.
+template <int PASS, bool STAGED = false>
 __global__ void __launch_bounds__(128) ref_expand(RefArgs r) {
+  extern __shared__ float s_stage[];
   const int lane = threadIdx.x & 31;
+  float *wstage = STAGED ? s_stage + (size_t)(threadIdx.x >> 5) * r.Z * 24 : nullptr;
   const int64_t ij = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (ij >= r.n2d * r.P) return;        // uniform per warp
   const int64_t i = ij / r.P;
@@ -234,7 +293,8 @@ __global__ void __launch_bounds__(128) ref_expand(RefArgs r) {
           bool h2;
           const int64_t t = ij * r.Z + k;
           track_segment<true>(r, pos, cos_d, s_full, zz, last_seg, k, &h2,
-                              r.off[t] + cst[k], r.ij_base[ij] + local + (incl - cm));
+                              r.off[t] + cst[k], r.ij_base[ij] + local + (incl - cm),
+                              STAGED ? wstage + (size_t)k * 24 : nullptr, r.off[t]);
           zst[k] = zz;
           cst[k] += c;
         }
@@ -253,6 +313,14 @@ __global__ void __launch_bounds__(128) ref_expand(RefArgs r) {
       begin += hits;                     // src/solver.c:468-469
   }
   if (PASS == 0 && lane == 0) r.ij_tot[ij] = local;
+  if (PASS == 1 && STAGED) {
+    // the last, partly filled group of every ray
+    __syncwarp();
+    for (int k = lane; k < r.Z; k += 32) {
+      const int64_t first = r.off[ij * r.Z + k], end = first + cst[k];
+      if (end > first && (end & 7) != 0) stage_flush(r, wstage + (size_t)k * 24, first, end);
+    }
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -276,6 +344,7 @@ struct RefState {
   int64_t cap = 0;
   int64_t sweeps = 0;
   int64_t last_segments = 0;
+  double last_rng_ms = 0.0;
 };
 
 std::mutex g_mu;
@@ -526,11 +595,15 @@ int sweep_ref(int64_t *segments) {
     RTRY(dmalloc(&r.d_rng, cap));
     r.cap = cap;
   }
+  r.last_rng_ms = 0.0;
   if (g_rng_mode == MOC_REF_RNG_LIBC && M > 0) {
     // the serial reference draws rand() once per sub-segment in traversal
     // order (src/solver.c:481); the same draws, from the process's libc state
+    const auto t0 = std::chrono::steady_clock::now();
     std::vector<int32_t> rv((size_t)M);
     for (int64_t k = 0; k < M; ++k) rv[(size_t)k] = rand();
+    r.last_rng_ms =
+        std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
     MOC_CUDA_TRY(cudaMemcpyAsync(r.d_rng, rv.data(), sizeof(int32_t) * (size_t)M,
                                  cudaMemcpyHostToDevice, st));
     MOC_CUDA_TRY(cudaStreamSynchronize(st));
@@ -538,7 +611,17 @@ int sweep_ref(int64_t *segments) {
   MOC_CUDA_TRY(cudaMemcpyAsync(r.d_ij_base, base.data(), sizeof(int64_t) * (size_t)pairs,
                                cudaMemcpyHostToDevice, st));
   MOC_CUDA_TRY(cudaMemcpyAsync(r.d_off + r.n3d, &M, sizeof(int64_t), cudaMemcpyHostToDevice, st));
-  ref_expand<1><<<grid, 128, 0, st>>>(make_args(r, r.d_z));
+  // pass 1 with staged stores: one warp a block, 96 bytes of groups per ray
+  const size_t stage_bytes = (size_t)96 * r.Z;
+  if (stage_bytes <= (size_t)200 * 1024) {
+    if (stage_bytes > 48 * 1024)
+      MOC_CUDA_TRY(cudaFuncSetAttribute(ref_expand<1, true>,
+                                        cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        (int)stage_bytes));
+    ref_expand<1, true><<<(unsigned)pairs, 32, stage_bytes, st>>>(make_args(r, r.d_z));
+  } else {
+    ref_expand<1><<<grid, 128, 0, st>>>(make_args(r, r.d_z));
+  }
   MOC_CUDA_TRY(cudaGetLastError());
   const bool had_pending = r.p->psi_pending;
   RTRY(moc_launch_sweep_csr(r.p, r.d_off, r.d_sds, r.d_sz, r.d_ssrc));
@@ -656,5 +739,7 @@ void moc_ref_finalize(void) {
 int moc_ref_status(void) { return g_status; }
 
 int64_t moc_ref_last_segments(void) { return g_ref.last_segments; }
+
+double moc_ref_last_rng_ms(void) { return g_ref.last_rng_ms; }
 
 }  // extern "C"

@@ -946,17 +946,26 @@ __global__ void __launch_bounds__(BLOCK, 2) sweep_batch_kernel(const SweepArgs *
     for (int i = threadIdx.x; i < table_n; i += BLOCK) s_table[i] = table[i];
     __syncthreads();
   }
+  // the task's core arguments, one slot per warp: the sweep reads its fields
+  // from shared memory instead of holding the whole struct in registers
+  __shared__ SweepArgs s_args[BLOCK / 32];
   const int lane = threadIdx.x & 31;
+  SweepArgs &a = s_args[threadIdx.x >> 5];
   for (;;) {
     unsigned long long t = 0;
     if (lane == 0) t = atomicAdd(counter, 1ull);
     t = __shfl_sync(FULL, t, 0);
     if (t >= (unsigned long long)n_tasks) break;
     const int2 task = tasks[t];
-    const SweepArgs a = cores[task.x];        // by value: the fields live in registers
+    static_assert(sizeof(SweepArgs) % 4 == 0, "the arguments copy as 4-byte words");
+    const uint32_t *src = reinterpret_cast<const uint32_t *>(cores + task.x);
+    uint32_t *dst = reinterpret_cast<uint32_t *>(&a);
+    for (int i = lane; i < (int)(sizeof(SweepArgs) / 4); i += 32) dst[i] = __ldg(src + i);
+    __syncwarp();
     const int tpw = core_tpw[task.x];
     sweep_track<0, BATCH_CPL, MODE, QUAD, false>(a, (int64_t)task.y + lane / tpw, lane, tpw,
                                                  s_table);
+    __syncwarp();                             // every lane is done with the slot
   }
 }
 

@@ -98,6 +98,8 @@ def lib() -> C.CDLL:
         lb.moc_ref_status.restype = C.c_int
         lb.moc_ref_last_segments.argtypes = []
         lb.moc_ref_last_segments.restype = C.c_int64
+        lb.moc_ref_last_rng_ms.argtypes = []
+        lb.moc_ref_last_rng_ms.restype = C.c_double
         _BOUND = True
     return lb
 
