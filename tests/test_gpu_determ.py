@@ -63,7 +63,8 @@ def test_mixed_runs_are_identical(gpu_available, axial_exp):
     with sm.Solver(hp, mode="mixed") as s:
         h = s.run(3)
         o = s.download(fine_flux=True, fine_source=True, psi_f=True)
-    assert abs(h[-1][0] - hists[0][-1][0]) <= 1e-6 * abs(h[-1][0])
+    # k_eff is a ratio of sums of the fluxes: the same tally-order tolerance
+    assert abs(h[-1][0] - hists[0][-1][0]) <= 1e-5 * abs(h[-1][0])
     for k in ("fine_flux", "fine_source", "psi_f"):
         assert rel_err(outs[0][k], o[k]) <= 1e-5, k
 
