@@ -326,13 +326,15 @@ def run_reference(args, spec):
     print(json.dumps(line), flush=True)
 
 
-def _traffic_from_profiles():
-    """Per-launch DRAM bytes of the sweep kernel from the committed ncu summary."""
+def _traffic_from_profiles(shape):
+    """Per-launch DRAM bytes of the sweep kernel of launch shape (tpw, cpl) from the
+    committed ncu summary, None if that shape was not captured."""
     p = ROOT / "profiles" / "sweep_default_traffic.txt"
-    if not p.exists():
+    if not p.exists() or shape is None:
         return None
+    key = f"dram_bytes_per_launch_full_size[{shape[0]}x{shape[1]}]"
     for ln in p.read_text().splitlines():
-        if ln.startswith("dram_bytes_per_launch_full_size"):
+        if ln.startswith(key):
             try:
                 return float(ln.split("=")[1].split()[0])
             except (IndexError, ValueError):
@@ -663,7 +665,8 @@ def main():
     peak, peak_kind = _peaks()
     alg_bytes = spec.algorithmic_bytes()
     achieved = alg_bytes / (sweep_ms / 1e3) / 1e9
-    traffic = _traffic_from_profiles() if args.config == "default" else None
+    traffic = (_traffic_from_profiles(tuple(shapes["mixed"])) if args.config == "default"
+               else None)
     if rank == 0:
         line = {
             "metric": METRIC,
@@ -682,6 +685,8 @@ def main():
             "sweep_ms": sweep_ms, "keff": r["keff"], "launch_shape": shapes,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
+                         "traffic_source": "ncu of the chosen launch shape on 1024 of the 2D "
+                                           "tracks, scaled to the full launch",
                          "peak_source": peak_kind,
                          "algorithmic_bytes_per_launch": alg_bytes},
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,

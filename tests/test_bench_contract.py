@@ -33,6 +33,8 @@ def test_reference_arm_line(lib, port):
     cb = d["cpu_baseline"]
     assert cb["value"] == d["value"] and cb["unit"] == d["unit"]
     assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["sample"]
+    # timed with the reference's own timing flags (src/Makefile:77), stated in the line
+    assert "-Ofast" in d["config"]["compiler_flags"] and "-fopenmp" in cb["compiler_flags"]
     e2e = d["e2e"]
     assert e2e["value"] == d["value"] and e2e["unit"] == d["unit"]
     assert e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
@@ -40,3 +42,20 @@ def test_reference_arm_line(lib, port):
 
 def test_reference_arm_other_ranks_exit_quietly(lib, port):
     assert _run({"RANK": "1", "LOCAL_RANK": "1", "WORLD_SIZE": "2"}) == []
+
+
+def test_flux_error_figures():
+    """bench.flux_errors: normwise, per FSR (max norm over its groups) and per
+    element, on a case with known answers."""
+    import numpy as np
+
+    import bench
+    ref = np.array([1.0, 2.0, 4.0, 8.0, 1.0, 1.0])        # two FSRs of three groups
+    a = ref.copy()
+    a[1] += 1e-3                                          # FSR 0: 1e-3 / 4
+    a[4] += 2e-3                                          # FSR 1: 2e-3 / 8
+    e = bench.flux_errors(a, ref, 3)
+    assert abs(e["normwise"] - 2e-3 / 8) < 1e-15
+    assert abs(e["per_fsr_max"] - 2.5e-4) < 1e-15
+    assert abs(e["per_element_max"] - 2e-3) < 1e-15
+    assert e["per_fsr_frac_within_contract"] == 0.0
