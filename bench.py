@@ -406,6 +406,8 @@ def run_adjoint(args):
     fixed-source sweep and its reverse sweep (psi checkpoints every 8
     segments).  Reports forward, forward-with-checkpoints and reverse times
     (events on the library stream, via the C ABI) and their ratio."""
+    import ctypes as C
+
     import torch
 
     import simplemoc_gb300 as sm
@@ -421,23 +423,15 @@ def run_adjoint(args):
         s.time_sweep(max(1, W))
         t_fwd = s.time_sweep(K)
         dphi = torch.rand(spec.n_fsr * spec.n_groups, device=dev)
-        dq = torch.empty_like(dphi)
-        dsig = torch.empty(hp.sigt.size, dtype=torch.float64, device=dev)
-        ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        torch.cuda.synchronize()
+        fms, rms = C.c_double(), C.c_double()
         fw, rv = [], []
         for it in range(W + K):
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            L.check(lib.moc_adjoint_forward(h, 8), "moc_adjoint_forward")
-            s.synchronize()
-            t1 = time.perf_counter()
-            L.check(lib.moc_adjoint_backward(h, dphi.data_ptr(), dq.data_ptr(), dsig.data_ptr(),
-                                             None), "moc_adjoint_backward")
-            s.synchronize()
-            t2 = time.perf_counter()
+            L.check(lib.moc_time_adjoint(h, 8, dphi.data_ptr(), C.byref(fms), C.byref(rms)),
+                    "moc_time_adjoint")
             if it >= W:
-                fw.append((t1 - t0) * 1e3)
-                rv.append((t2 - t1) * 1e3)
+                fw.append(fms.value)
+                rv.append(rms.value)
     f, r = float(np.median(fw)), float(np.median(rv))
     line = {
         "metric": "adjoint sweep time / forward sweep time", "value": (f + r) / t_fwd,

@@ -363,6 +363,11 @@ int moc_set_cross_sections(moc_problem *p, const float *xs, const float *scatter
 /* The scalar flux from / the fine source to device arrays (row stride G). */
 int moc_set_fine_flux_device(moc_problem *p, const float *phi);
 int moc_get_fine_source_device(moc_problem *p, float *q);
+/* Device time (events on the handle's stream) of one moc_adjoint_forward(k_ckpt)
+ * and of the reverse sweep that follows it for dL/dphi (device [NS*F*G]), in
+ * milliseconds; the gradients stay in the handle's work arrays. */
+int moc_time_adjoint(moc_problem *p, int k_ckpt, const float *dphi, double *ms_forward,
+                     double *ms_reverse);
 /* Lanes per track (1..32, any width) and 4-group chunks per lane (1 or 2) of
  * the reverse sweep; 0, 0 = automatic (ceil(G/4) lanes of one chunk up to 128
  * groups).  MOC_ERR_ARG when lanes x chunks x 4 < G. */

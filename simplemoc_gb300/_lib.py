@@ -122,6 +122,7 @@ SIGNATURES = {
     "moc_adjoint_backward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                        C.c_void_p]),
     "moc_set_adjoint_width": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "moc_time_adjoint": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, f64p, f64p]),
     "moc_update_sources_adjoint": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_double,
                                              C.c_void_p, C.c_void_p, C.c_void_p]),
     "moc_set_cross_sections": (C.c_int, [C.c_void_p, f32p, f32p]),

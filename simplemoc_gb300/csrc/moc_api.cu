@@ -1314,4 +1314,30 @@ int moc_adjoint_backward(moc_problem *p, const float *dphi, float *dq, double *d
   return moc_adjoint_backward_fit(p, dphi, dq, dsigt, dpsi_in, nullptr);
 }
 
+int moc_time_adjoint(moc_problem *p, int k_ckpt, const float *dphi, double *ms_forward,
+                     double *ms_reverse) {
+  int rc = ready(p);
+  if (rc != MOC_OK) return rc;
+  if (!dphi || !ms_forward || !ms_reverse) return MOC_ERR_ARG;
+  cudaSetDevice(p->device);
+  cudaEvent_t mid = nullptr;
+  if (cudaEventCreate(&mid) != cudaSuccess) return fail(p, MOC_ERR_CUDA);
+  if (cudaEventRecord(p->ev0, p->stream) != cudaSuccess) rc = MOC_ERR_CUDA;
+  if (rc == MOC_OK) rc = moc_adjoint_forward(p, k_ckpt);
+  if (rc == MOC_OK && cudaEventRecord(mid, p->stream) != cudaSuccess) rc = MOC_ERR_CUDA;
+  if (rc == MOC_OK) rc = moc_adjoint_backward_fit(p, dphi, nullptr, nullptr, nullptr, nullptr);
+  if (rc == MOC_OK && cudaEventRecord(p->ev1, p->stream) != cudaSuccess) rc = MOC_ERR_CUDA;
+  if (rc == MOC_OK && cudaEventSynchronize(p->ev1) != cudaSuccess) rc = MOC_ERR_CUDA;
+  float f = 0.f, r = 0.f;
+  if (rc == MOC_OK) {
+    cudaEventElapsedTime(&f, p->ev0, mid);
+    cudaEventElapsedTime(&r, mid, p->ev1);
+  }
+  cudaEventDestroy(mid);
+  if (rc != MOC_OK) return rc == MOC_ERR_CUDA ? fail(p, rc) : rc;
+  *ms_forward = f;
+  *ms_reverse = r;
+  return sync_check(p);
+}
+
 }  // extern "C"
