@@ -185,25 +185,38 @@ struct Seg {
   int64_t crow;   // coefficient block
 };
 
+// FMA_ZIN (MIXED and the adjoint): the height within the fitted interval in one
+// rounding, zin = RN(z - dz (centre)), with the edge shift folded into the
+// centre.  The reference's float expression (PLAIN) rounds the product
+// dz (zi + 1/2) of a height of up to the domain's (hundreds of cm) and then the
+// difference and the shift: an absolute error of ~1e-5 cm in a zin of a few cm,
+// which reaches the quadratic fit's q0 and q1 at ~1e-6 relative and was the
+// largest error of the MIXED sweep against FP64.
+template <bool FMA_ZIN = false>
 __device__ __forceinline__ Seg segment_geometry(const SweepArgs &a, float z, int s) {
   Seg g;
   // src/solver.c:38-45 (z / dz once: both uses are the same expression)
   int zi = __float2int_rz(div_cr(z, a.dz, a.rdz));
-  float zin = __fsub_rn(z, __fmul_rn(a.dz, __fadd_rn(__int2float_rn(zi), 0.5f)));
+  const float centre = __fadd_rn(__int2float_rn(zi), 0.5f);      // exact below 2^23
+  float zin = FMA_ZIN ? 0.f : __fsub_rn(z, __fmul_rn(a.dz, centre));
   // zi % F by a multiply-high; the host verified the magic over every reachable zi
   int fine = a.fmagic ? zi - a.F * (int)__umulhi((unsigned)zi, a.fmagic) : zi % a.F;
   int r0 = fine;
+  float shift = 0.f;
   if (a.axial_exp == 2) {
     if (fine == 0) {                     // src/solver.c:55-58
-      zin = __fsub_rn(zin, a.dz);
+      if (!FMA_ZIN) zin = __fsub_rn(zin, a.dz);
+      shift = 1.f;
       r0 = 0;
     } else if (fine == a.F - 1) {        // src/solver.c:84-87
-      zin = __fadd_rn(zin, a.dz);
+      if (!FMA_ZIN) zin = __fadd_rn(zin, a.dz);
+      shift = -1.f;
       r0 = fine - 2;
     } else {
       r0 = fine - 1;
     }
   }
+  if (FMA_ZIN) zin = __fmaf_rn(-a.dz, __fadd_rn(centre, shift), z);
   g.zin = zin;
   int64_t base = (int64_t)s * a.F;
   g.qrow = (base + r0) * a.ldg;
@@ -468,7 +481,7 @@ __device__ __forceinline__ void sweep_track(const SweepArgs &a, int64_t track, i
   }
 
   float ds = tshfl(ds_c, 0);
-  Seg g = segment_geometry(a, z, checked_source(a, tshfl(src_c, 0), li));
+  Seg g = segment_geometry<MODE == MODE_MIXED>(a, z, checked_source(a, tshfl(src_c, 0), li));
   int S_loop = S;                        // the warp's longest track (CSR, several a warp)
   if (CSR && TPW < 32) S_loop = (int)__reduce_max_sync(FULL, (unsigned)S);
   const uint64_t tally_pol = MODE == MODE_MIXED ? l2_evict_last_policy() : 0;
@@ -514,7 +527,7 @@ __device__ __forceinline__ void sweep_track(const SweepArgs &a, int64_t track, i
       }
       if (CSR) z_next = tshfl(z_c, k);
       ds1 = tshfl(ds_c, k);
-      g1 = segment_geometry(a, z_next, checked_source(a, tshfl(src_c, k), li));
+      g1 = segment_geometry<MODE == MODE_MIXED>(a, z_next, checked_source(a, tshfl(src_c, k), li));
       load_rows<CPL, QUAD, VW, L1A>(a, g1, li, TPW, rows1, nch);
     }
     // ---- segment n
@@ -780,7 +793,7 @@ __global__ void __launch_bounds__(BLOCK) sweep_staged_kernel(SweepArgs a, int ro
     }
     const float ds = __shfl_sync(FULL, ds_c, k, TPW);
     const int src = __shfl_sync(FULL, src_c, k, TPW);
-    const Seg g = segment_geometry(a, pz, checked_source(a, src, li));
+    const Seg g = segment_geometry<MODE == MODE_MIXED>(a, pz, checked_source(a, src, li));
     const int slot = (int)(issued % NST);
     if (li == 0) {
       StageGeo sg;
@@ -1684,7 +1697,7 @@ __global__ void __launch_bounds__(BLOCK, 2) adjoint_kernel(AdjArgs x) {
       // before its own arithmetic.
       float z = a.ck_z[tr * NCK + b];
       float ds = __ldg(dsb + n0);
-      Seg g = segment_geometry(a, z, checked_source(a, __ldg(srcb + n0), li));
+      Seg g = segment_geometry<true>(a, z, checked_source(a, __ldg(srcb + n0), li));
       AdjRows<CPL, QUAD> cur;
 #pragma unroll 1
       for (int jj = 0; jj < cnt; ++jj) {
@@ -1715,7 +1728,7 @@ __global__ void __launch_bounds__(BLOCK, 2) adjoint_kernel(AdjArgs x) {
         if (jj + 1 < cnt) {
           z = advance_z(a, z, ds, mu);
           ds = __ldg(dsb + n0 + jj + 1);
-          g = segment_geometry(a, z, checked_source(a, __ldg(srcb + n0 + jj + 1), li));
+          g = segment_geometry<true>(a, z, checked_source(a, __ldg(srcb + n0 + jj + 1), li));
         }
       }
       __syncwarp();
