@@ -361,10 +361,15 @@ int upload_all(moc_problem *p, const moc_host *h, bool stream_tracks) {
   }
   p->psi_pending = false;
   TRY(moc_reset_psi_scale(p));
-  if (stream_tracks)
+  if (!h->psi_b) {
+    // zeros by definition: no scan of the (cleared) array needed
+    p->detect_pending = false;
+    MOC_CUDA_TRY(cudaMemsetAsync(p->psi_b_nonzero, 0, sizeof(int32_t), p->stream));
+  } else if (stream_tracks) {
     p->detect_pending = true;          // psi_b is still being copied
-  else
+  } else {
     TRY(moc_detect_psi_b(p));
+  }
   MOC_CUDA_TRY(cudaMemsetAsync(p->err, 0, sizeof(int32_t), p->stream));
   return MOC_OK;
 }

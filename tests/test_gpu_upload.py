@@ -186,3 +186,26 @@ def test_streamed_upload_without_room_for_the_flux_side_buffer(gpu_available):
             L.check(lib.moc_set_memory_limit(0), "limit")
     assert np.array_equal(ra["psi_f"], rb["psi_f"])
     assert rel_err(rb["fine_flux"], ra["fine_flux"]) <= 1e-5
+
+
+def test_streamed_upload_of_null_backward_flux_gives_zeros(gpu_available):
+    """psi_b passed as NULL to a streamed upload means zeros: it replaces a
+    non-zero psi_b on the device, and two power iterations then equal those of
+    an upload with a zero array."""
+    from dataclasses import replace
+
+    import simplemoc_gb300 as sm
+    hp = _problem()                                      # psi_b non-zero
+    zero_b = hp.copy_state()
+    zero_b.psi_b[:] = 0.0
+    null_b = replace(hp.copy_state(), psi_b=None)
+    with sm.Solver(hp) as a, sm.Solver(hp) as b:
+        a.upload(null_b)
+        b.upload(zero_b)
+        ha, hb = a.run(2), b.run(2)
+        oa = a.download(fine_flux=True, fine_source=True, psi_f=True, psi_b=True)
+        ob = b.download(fine_flux=True, fine_source=True, psi_f=True, psi_b=True)
+    assert not oa["psi_b"].any()
+    assert abs(ha[-1][0] - hb[-1][0]) <= 1e-5 * abs(hb[-1][0])
+    for k in ("fine_flux", "fine_source", "psi_f"):
+        assert rel_err(oa[k], ob[k]) <= 1e-5, k
