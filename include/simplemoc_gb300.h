@@ -195,6 +195,7 @@ int64_t moc_device_bytes(const moc_problem *p);
 int moc_set_mode(moc_problem *p, int mode, int flags);
 /* Threads per track (4, 8, 16 or 32) and 4-group chunks per thread (1, 2, 4)
  * for the sweep kernel, or 10 threads x 5 two-group chunks (up to 100 groups,
+ * three tracks a warp), or 10 threads x 1 four-group chunk (up to 40 groups,
  * three tracks a warp); 0, 0 = pick automatically (autotuner choice). */
 int moc_set_launch(moc_problem *p, int threads_per_track, int chunks_per_thread);
 int moc_get_launch(const moc_problem *p, int *threads_per_track,

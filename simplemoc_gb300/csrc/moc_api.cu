@@ -800,7 +800,7 @@ int moc_set_launch(moc_problem *p, int threads_per_track, int chunks_per_thread)
     return MOC_OK;
   }
   static const int ok[][2] = {{32, 1}, {32, 2}, {32, 4}, {16, 1}, {16, 2}, {8, 1}, {8, 4}, {4, 2},
-                              {10, 5}};
+                              {10, 5}, {10, 1}};
   for (auto &s : ok) {
     if (s[0] == threads_per_track && s[1] == chunks_per_thread) {
       if (moc_shape_groups(threads_per_track, chunks_per_thread) < p->ldg) return MOC_ERR_ARG;

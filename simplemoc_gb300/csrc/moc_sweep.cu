@@ -1124,6 +1124,8 @@ int dispatch_shape(moc_problem *p, const SweepArgs &a, int tpw, int cpl) {
   if (tpw == 8 && cpl == 4) return launch_t<8, 4, MODE, QUAD>(p, a);
   if (tpw == 4 && cpl == 2) return launch_t<4, 2, MODE, QUAD>(p, a);
   if (tpw == 10 && cpl == 5) return launch_t<10, 5, MODE, QUAD, false, false, 2>(p, a);
+  // 10 lanes x one 4-group chunk: up to 40 groups, three tracks a warp
+  if (tpw == 10 && cpl == 1) return launch_t<10, 1, MODE, QUAD>(p, a);
   return MOC_ERR_UNSUPPORTED;
 }
 
@@ -1175,7 +1177,7 @@ int dispatch_staged(moc_problem *p, const SweepArgs &a, int tpw, int cpl, int st
 // launch-shape measurements on GB300 (two tracks per warp with two chunks per
 // thread was fastest for 100 groups in both modes); moc_autotune measures.
 int moc_shape_groups(int tpw, int cpl) {
-  return tpw * cpl * ((tpw & (tpw - 1)) == 0 ? 4 : 2);
+  return tpw * cpl * ((tpw == 10 && cpl == 5) ? 2 : 4);
 }
 
 int moc_sweep_launch_shape(const moc_problem *p, int *tpw, int *cpl) {
@@ -1391,7 +1393,8 @@ int moc_sweep_autotune(moc_problem *p, int64_t n_sub, int *tpw_out, int *cpl_out
     rc = MOC_ERR_CUDA;
   // register-prefetch shapes, then the staged kernel (4-stage ring) shapes
   static const int shapes[][3] = {{32, 1, 0}, {32, 2, 0}, {32, 4, 0}, {16, 1, 0}, {16, 2, 0},
-                                  {8, 1, 0},  {8, 4, 0},  {4, 2, 0},  {10, 5, 0}, {32, 1, 4},
+                                  {8, 1, 0},  {8, 4, 0},  {4, 2, 0},  {10, 5, 0}, {10, 1, 0},
+                                  {32, 1, 4},
                                   {32, 2, 4}, {16, 1, 4}, {16, 2, 4}, {8, 1, 4}};
   double best = 1e30;
   int bt = 0, bc = 0, bs = 0;
@@ -1872,6 +1875,8 @@ template <bool QUAD>
 int dispatch_ckpt(moc_problem *p, const SweepArgs &a) {
   const int nchunk = p->ldg / 4;
   if (nchunk <= 8) return launch_t<8, 1, MODE_MIXED, QUAD, false, true>(p, a);
+  // 33 to 40 groups: 10 lanes of one 4-group chunk, three tracks a warp
+  if (p->ldg <= 40) return launch_t<10, 1, MODE_MIXED, QUAD, false, true>(p, a);
   // 33 to 100 groups: two-group chunks, three tracks a warp (the forward sweep's
   // 10 x 5 shape; 16 lanes of float4 chunks would leave most of them idle)
   if (p->ldg <= 100) return launch_t<10, 5, MODE_MIXED, QUAD, false, true, 2>(p, a);

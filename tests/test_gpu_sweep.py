@@ -68,11 +68,12 @@ def _spec(**kw):
     return sm.ProblemSpec(**base)
 
 
-# (10, 5): chunks of two groups, 10 lanes x 5 chunks = 100 groups, three tracks a warp
-SHAPES = [(32, 1), (32, 2), (32, 4), (16, 1), (16, 2), (8, 1), (8, 4), (4, 2), (10, 5)]
+# (10, 5): chunks of two groups, 10 lanes x 5 chunks = 100 groups, three tracks a warp;
+# (10, 1): one chunk of four groups, 10 lanes = 40 groups, three tracks a warp
+SHAPES = [(32, 1), (32, 2), (32, 4), (16, 1), (16, 2), (8, 1), (8, 4), (4, 2), (10, 5), (10, 1)]
 
 
-@pytest.mark.parametrize("groups", [100, 7, 32, 20, 98])
+@pytest.mark.parametrize("groups", [100, 7, 32, 20, 98, 40, 37])
 def test_plain_every_launch_shape_bit_exact(gpu_available, port, groups):
     import simplemoc_gb300 as sm
     spec = _spec(n_groups=groups, n_tracks_2d=16, z_stacked=10)
@@ -83,7 +84,7 @@ def test_plain_every_launch_shape_bit_exact(gpu_available, port, groups):
     ldg = (groups + 3) // 4 * 4
     ran = 0
     for tpw, cpl in SHAPES:
-        vw = 4 if tpw & (tpw - 1) == 0 else 2          # chunk width: groups per lane chunk
+        vw = 2 if (tpw, cpl) == (10, 5) else 4         # chunk width: groups per lane chunk
         if tpw * cpl * vw < ldg:
             continue
         with _solver(hp) as s:
