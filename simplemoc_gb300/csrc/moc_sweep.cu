@@ -369,6 +369,31 @@ __device__ __forceinline__ void comp_add_vec(float *hi, float *lo, float2 t) {
                "f"(two_sum_err(o.y, t.y)));
 }
 
+// The returning vector atomic of a compensated chunk: the old hi words.
+__device__ __forceinline__ float4 atom_add_vec(float *hi, float4 t) {
+  float4 o;
+  asm volatile("atom.global.v4.f32.add {%0,%1,%2,%3}, [%4], {%5,%6,%7,%8};"
+               : "=f"(o.x), "=f"(o.y), "=f"(o.z), "=f"(o.w)
+               : "l"(hi), "f"(t.x), "f"(t.y), "f"(t.z), "f"(t.w)
+               : "memory");
+  return o;
+}
+__device__ __forceinline__ float2 atom_add_vec(float *hi, float2 t) {
+  float2 o;
+  asm volatile("atom.global.v2.f32.add {%0,%1}, [%2], {%3,%4};"
+               : "=f"(o.x), "=f"(o.y)
+               : "l"(hi), "f"(t.x), "f"(t.y)
+               : "memory");
+  return o;
+}
+__device__ __forceinline__ float4 two_sum_err(float4 o, float4 t) {
+  return make_float4(two_sum_err(o.x, t.x), two_sum_err(o.y, t.y), two_sum_err(o.z, t.z),
+                     two_sum_err(o.w, t.w));
+}
+__device__ __forceinline__ float2 two_sum_err(float2 o, float2 t) {
+  return make_float2(two_sum_err(o.x, t.x), two_sum_err(o.y, t.y));
+}
+
 // Loads of one segment that are issued one segment ahead (software pipeline):
 // the three fine-source rows (one row for the flat source) of every chunk.
 template <int CPL, bool QUAD, int VW = 4>
@@ -412,7 +437,7 @@ __device__ __forceinline__ int checked_source(const SweepArgs &a, int s, int li)
 // the threads per track when known at compile time; 0 takes tpw_rt (the
 // batched kernel, where each core has its own width).
 template <int TPW_CT, int CPL, int MODE, bool QUAD, bool CSR, bool CKPT = false, int VW = 4,
-          bool REC = false>
+          bool REC = false, bool COMP = false>
 __device__ __forceinline__ void sweep_track(const SweepArgs &a, int64_t track, int lane,
                                             int tpw_rt, const float2 *s_table) {
   const int TPW = TPW_CT ? TPW_CT : tpw_rt;
@@ -488,6 +513,12 @@ __device__ __forceinline__ void sweep_track(const SweepArgs &a, int64_t track, i
   Rows<CPL, QUAD, VW> rows;
   if (S_loop > 0) load_rows<CPL, QUAD, VW, L1A>(a, g, li, TPW, rows, nch);
 
+  // COMP: the compensation of each chunk's tallies waits one segment, so that
+  // the returning atomic's old values arrive under the next segment's work
+  V pend_o[COMP ? CPL : 1], pend_t[COMP ? CPL : 1];
+  int64_t pend_off[COMP ? CPL : 1];
+#pragma unroll
+  for (int k = 0; k < (COMP ? CPL : 1); ++k) pend_off[k] = -1;
   int ck_left = 0;                       // segments to the next checkpoint
   int64_t ck_slot = CKPT ? tr * a.ck_n : 0;
   for (int n = 0; n < S_loop; ++n) {
@@ -600,11 +631,18 @@ __device__ __forceinline__ void sweep_track(const SweepArgs &a, int64_t track, i
           *reinterpret_cast<V *>(a.rec + slot * a.ldg + g4) = t;
           if (c == 0) a.rec_row[slot] = (int32_t)(g.frow / a.ldg);
         }
+      } else if (COMP) {
+        if (valid) {
+          const int64_t off = g.frow + g4;
+          const V o = atom_add_vec(a.phi + off, t);
+          if (pend_off[k] >= 0) red_add_vec(a.phi_lo + pend_off[k], two_sum_err(pend_o[k], pend_t[k]));
+          pend_o[k] = o;
+          pend_t[k] = t;
+          pend_off[k] = off;
+        }
       } else if (valid) {
         float *dst = a.phi + g.frow + g4;
-        if (MODE == MODE_MIXED && a.phi_lo != nullptr) {
-          comp_add_vec(dst, a.phi_lo + g.frow + g4, t);
-        } else if (MODE == MODE_MIXED) {
+        if (MODE == MODE_MIXED) {
           red_add_vec_last(dst, t, tally_pol);
         } else {
           red_add_vec(dst, t);
@@ -615,6 +653,11 @@ __device__ __forceinline__ void sweep_track(const SweepArgs &a, int64_t track, i
     ds = ds1;
     g = g1;
     rows = rows1;
+  }
+  if (COMP) {
+#pragma unroll
+    for (int k = 0; k < (COMP ? CPL : 1); ++k)
+      if (pend_off[k] >= 0) red_add_vec(a.phi_lo + pend_off[k], two_sum_err(pend_o[k], pend_t[k]));
   }
   if (valid) {
 #pragma unroll
@@ -628,7 +671,8 @@ __device__ __forceinline__ void sweep_track(const SweepArgs &a, int64_t track, i
 // With TPW not dividing 32 the last 32 % TPW lanes own no track: they run the
 // loop on an out-of-range track (loads clamped to a real one, no stores) so that
 // the warp's shuffles stay converged.
-template <int TPW, int CPL, int MODE, bool QUAD, bool CSR, bool CKPT, int VW, bool REC = false>
+template <int TPW, int CPL, int MODE, bool QUAD, bool CSR, bool CKPT, int VW, bool REC = false,
+          bool COMP = false>
 __device__ __forceinline__ void sweep_body(const SweepArgs &a, float2 *s_table) {
   if (MODE == MODE_PLAIN) {
     for (int i = threadIdx.x; i < a.table_n; i += BLOCK) s_table[i] = a.table[i];
@@ -640,7 +684,7 @@ __device__ __forceinline__ void sweep_body(const SweepArgs &a, float2 *s_table) 
   const int64_t warp_id = ((int64_t)blockIdx.x * BLOCK + threadIdx.x) >> 5;
   const int64_t n_warps = ((int64_t)gridDim.x * BLOCK) >> 5;
   for (int64_t base = warp_id * GPW; base < a.n3d; base += n_warps * GPW)
-    sweep_track<TPW, CPL, MODE, QUAD, CSR, CKPT, VW, REC>(a, gw < GPW ? base + gw : a.n3d, lane,
+    sweep_track<TPW, CPL, MODE, QUAD, CSR, CKPT, VW, REC, COMP>(a, gw < GPW ? base + gw : a.n3d, lane,
                                                           TPW, s_table);
 }
 
@@ -656,6 +700,15 @@ template <int TPW, int CPL, int MODE, bool QUAD>
 __global__ void __launch_bounds__(BLOCK) sweep_record_kernel(SweepArgs a) {
   extern __shared__ float2 s_table[];
   sweep_body<TPW, CPL, MODE, QUAD, false, false, 4, true>(a, s_table);
+}
+
+// MIXED with compensated tallies (MOC_FLAG_COMPENSATED): the hi words by a
+// returning vector atomic, their rounding errors one segment later into the lo
+// words (four-group chunks).
+template <int TPW, int CPL, bool QUAD>
+__global__ void __launch_bounds__(BLOCK) sweep_comp_kernel(SweepArgs a) {
+  extern __shared__ float2 s_table[];
+  sweep_body<TPW, CPL, MODE_MIXED, QUAD, false, false, 4, false, true>(a, s_table);
 }
 
 // Two-group chunks: held to two blocks an SM (the MIXED quadratic variant
@@ -1066,10 +1119,12 @@ __global__ void __launch_bounds__(BLOCK) sweep64_kernel(SweepArgs a) {
 }
 
 template <int TPW, int CPL, int MODE, bool QUAD, bool CSR = false, bool CKPT = false,
-          int VW = 4, bool REC = false>
+          int VW = 4, bool REC = false, bool COMP = false>
 int launch_t(moc_problem *p, const SweepArgs &a) {
   void (*kern)(SweepArgs);
-  if constexpr (REC)
+  if constexpr (COMP)
+    kern = sweep_comp_kernel<TPW, CPL, QUAD>;
+  else if constexpr (REC)
     kern = sweep_record_kernel<TPW, CPL, MODE, QUAD>;
   else if constexpr (VW == 4)
     kern = sweep_kernel<TPW, CPL, MODE, QUAD, CSR, CKPT>;
@@ -1126,6 +1181,28 @@ int dispatch_shape(moc_problem *p, const SweepArgs &a, int tpw, int cpl) {
   if (tpw == 10 && cpl == 5) return launch_t<10, 5, MODE, QUAD, false, false, 2>(p, a);
   // 10 lanes x one 4-group chunk: up to 40 groups, three tracks a warp
   if (tpw == 10 && cpl == 1) return launch_t<10, 1, MODE, QUAD>(p, a);
+  return MOC_ERR_UNSUPPORTED;
+}
+
+// The compensated MIXED sweep: power-of-two shapes of four-group chunks; any
+// other shape falls back to the narrowest of them that covers the groups.
+template <bool QUAD>
+int dispatch_comp(moc_problem *p, const SweepArgs &a, int tpw, int cpl) {
+  constexpr int M = MODE_MIXED;
+  if (tpw == 32 && cpl == 1) return launch_t<32, 1, M, QUAD, false, false, 4, false, true>(p, a);
+  if (tpw == 32 && cpl == 2) return launch_t<32, 2, M, QUAD, false, false, 4, false, true>(p, a);
+  if (tpw == 32 && cpl == 4) return launch_t<32, 4, M, QUAD, false, false, 4, false, true>(p, a);
+  if (tpw == 16 && cpl == 1) return launch_t<16, 1, M, QUAD, false, false, 4, false, true>(p, a);
+  if (tpw == 16 && cpl == 2) return launch_t<16, 2, M, QUAD, false, false, 4, false, true>(p, a);
+  if (tpw == 8 && cpl == 1) return launch_t<8, 1, M, QUAD, false, false, 4, false, true>(p, a);
+  if (tpw == 8 && cpl == 4) return launch_t<8, 4, M, QUAD, false, false, 4, false, true>(p, a);
+  if (tpw == 4 && cpl == 2) return launch_t<4, 2, M, QUAD, false, false, 4, false, true>(p, a);
+  const int nchunk = p->ldg / 4;
+  if (nchunk <= 8) return dispatch_comp<QUAD>(p, a, 8, 1);
+  if (nchunk <= 16) return dispatch_comp<QUAD>(p, a, 16, 1);
+  if (nchunk <= 32) return dispatch_comp<QUAD>(p, a, 16, 2);
+  if (nchunk <= 64) return dispatch_comp<QUAD>(p, a, 32, 2);
+  if (nchunk <= 128) return dispatch_comp<QUAD>(p, a, 32, 4);
   return MOC_ERR_UNSUPPORTED;
 }
 
@@ -1262,6 +1339,8 @@ int launch_args(moc_problem *p, const SweepArgs &a, int tpw, int cpl, int stages
   if (p->mode == MOC_MODE_PLAIN)
     return quad ? dispatch_shape<MODE_PLAIN, true>(p, a, tpw, cpl)
                 : dispatch_shape<MODE_PLAIN, false>(p, a, tpw, cpl);
+  if (a.phi_lo)
+    return quad ? dispatch_comp<true>(p, a, tpw, cpl) : dispatch_comp<false>(p, a, tpw, cpl);
   return quad ? dispatch_shape<MODE_MIXED, true>(p, a, tpw, cpl)
               : dispatch_shape<MODE_MIXED, false>(p, a, tpw, cpl);
 }
@@ -1402,6 +1481,7 @@ int moc_sweep_autotune(moc_problem *p, int64_t n_sub, int *tpw_out, int *cpl_out
     if (rc != MOC_OK) break;
     const int covered = moc_shape_groups(sh[0], sh[1]);
     if (covered < p->ldg) continue;
+    if (a.phi_lo && sh[0] == 10) continue;       // no compensated ten-lane variant
     if (covered >= 4 * p->ldg && sh[1] > 1) continue;                  // mostly idle lanes
     if (sh[2] > 0 && staged_smem(a, p->mode == MOC_MODE_PLAIN ? MODE_PLAIN : MODE_MIXED,
                                  p->d.axial_exp == 2, sh[0], sh[2]) > 227 * 1024)
