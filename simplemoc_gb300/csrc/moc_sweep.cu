@@ -1616,9 +1616,11 @@ struct AdjOut {
 };
 
 __device__ __forceinline__ AdjOut adj_quad(const SweepArgs &a, float y1, float y2, float y3,
-                                           float sig, float r1, float zin, float ds, float mu,
-                                           float mu2, float psi, float pbar, float abar) {
-  const float r2 = r1 * r1, r3 = r1 * r2, r4 = r2 * r2 * (1.0f / 3.0f);
+                                           float sig, float r1, float r2, float r3x2, float r4,
+                                           float zin, float ds, float mu, float mu2, float psi,
+                                           float pbar, float abar) {
+  // the coefficient planes 1/sigma^2, 2/sigma^3, 1/(3 sigma^4), as the forward
+  const float r3 = 0.5f * r3x2;
   const float c1 = (y1 - y3) * a.rd1;
   const float c2 = (fmaf(-2.f, y2, y1) + y3) * a.rd2;
   const float q0 = fmaf(fmaf(c2, zin, c1), zin, y2);
@@ -1691,16 +1693,18 @@ __device__ __forceinline__ void adj_load(const SweepArgs &a, const AdjArgs &x, c
     const float *cf = a.coef + g.crow + 4 * COEF_PLANES * c;
     r.sig[k] = __ldg(reinterpret_cast<const float4 *>(cf));
     r.r1[k] = __ldg(reinterpret_cast<const float4 *>(cf + 4));
-    if (!LAM && QUAD) {                 // the recomputation: the forward's planes
+    if (QUAD) {                         // the forward's planes, in both passes
       r.r2[k] = __ldg(reinterpret_cast<const float4 *>(cf + 8));
       r.r4[k] = __ldg(reinterpret_cast<const float4 *>(cf + 16));
       r.r3x2[k] = __ldg(reinterpret_cast<const float4 *>(cf + 20));
     }
-const float *qr = a.q + g.qrow + 4 * c;
-    r.y[k][0] = ld_stream(qr);
+    // the rows allocate in L1: the reverse pass reads the rows the
+    // recomputation read a few segments before
+    const float *qr = a.q + g.qrow + 4 * c;
+    ld_row_vec<true>(qr, r.y[k][0]);
     if (QUAD) {
-      r.y[k][QUAD ? 1 : 0] = ld_stream(qr + a.ldg);
-      r.y[k][QUAD ? 2 : 0] = ld_stream(qr + 2 * a.ldg);
+      ld_row_vec<true>(qr + a.ldg, r.y[k][QUAD ? 1 : 0]);
+      ld_row_vec<true>(qr + 2 * a.ldg, r.y[k][QUAD ? 2 : 0]);
     }
     if (LAM) r.lam[k] = __ldg(reinterpret_cast<const float4 *>(x.dphi + g.frow + 4 * c));
   }
@@ -1835,7 +1839,8 @@ __global__ void __launch_bounds__(BLOCK, 2) adjoint_kernel(AdjArgs x) {
             const AdjOut o =
                 QUAD ? adj_quad(a, get(cur.y[k][0], e), get(cur.y[k][QUAD ? 1 : 0], e),
                                 get(cur.y[k][QUAD ? 2 : 0], e), get(cur.sig[k], e),
-                                get(cur.r1[k], e), g.zin, ds, mu, mu2, get(ph, e),
+                                get(cur.r1[k], e), get(cur.r2[k], e), get(cur.r3x2[k], e),
+                                get(cur.r4[k], e), g.zin, ds, mu, mu2, get(ph, e),
                                 get(pbar[k], e), abar)
                      : adj_flat(get(cur.y[k][0], e), get(cur.sig[k], e), get(cur.r1[k], e), ds,
                                 get(ph, e), get(pbar[k], e), abar);
