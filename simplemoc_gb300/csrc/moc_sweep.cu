@@ -1612,52 +1612,55 @@ struct AdjArgs {
 
 struct AdjOut {
   float pbar, y1b, y2b, y3b, sbar;
-  float c0b, c1b, c2b;    // quadratic source: dL/d of the fit's c0, c1, c2
+  float q0b, q1mub, q2mu2b;   // quadratic source: dL/d q0, d(q1 mu), d(q2 mu^2)
 };
 
-__device__ __forceinline__ AdjOut adj_quad(const SweepArgs &a, float y1, float y2, float y3,
-                                           float sig, float r1, float r2, float r3x2, float r4,
-                                           float zin, float ds, float mu, float mu2, float psi,
-                                           float pbar, float abar) {
-  // the coefficient planes 1/sigma^2, 2/sigma^3, 1/(3 sigma^4), as the forward
-  const float r3 = 0.5f * r3x2;
-  const float c1 = (y1 - y3) * a.rd1;
-  const float c2 = (fmaf(-2.f, y2, y1) + y3) * a.rd2;
-  const float q0 = fmaf(fmaf(c2, zin, c1), zin, y2);
-  const float q1 = fmaf(2.f * c2, zin, c1);
-  const float q2 = c2;
+// Reverse of mixed_quad for one group.  With the per-segment fit factors f
+// (mixed_fit), E = 1 - e^-tau and the weights
+//   T = (tau - E)/sig^2, U = E/sig, R = tau (tau - 2) + 2E/sig^3 (the reference's
+//   reuse term), C = (tau^3 - 3 tau^2 + 6 tau - 6E)/(3 sig^4),
+// the forward is fi = q0 T + psi U + q1mu R + q2mu2 C and
+// pn = q0 U + q1mu T + q2mu2 R + psi (1 - E).  Given abar = dL/dfi (w dL/dphi) and
+// pbar = dL/dpn it returns dL/dpsi, dL/d of the three fit rows and of q0, q1 mu,
+// q2 mu^2, and dL/dsigma through the sigma-derivatives of the weights
+// (tau = sig ds, E' = ds (1 - E)):
+//   U' = (E' - U)/sig, T' = ds E/sig^2 - 2T/sig, R' = (2tau - 2) ds + 2/sig^3 (E' - 3U),
+//   C' = ((3tau^2 - 6tau + 6) ds - 6E')/(3 sig^4) - 4C/sig.
+__device__ __forceinline__ AdjOut adj_quad(float y1, float y2, float y3, const MixedFit &f,
+                                           float sig, float r1, float ds, float psi, float pbar,
+                                           float abar) {
+  const float r2 = r1 * r1, r3 = r1 * r2, r4 = r2 * r2 * (1.0f / 3.0f);
+  const float d1 = y1 - y3;
+  const float d2 = fmaf(-2.f, y2, y1) + y3;
+  const float q0 = fmaf(d2, f.a0, fmaf(d1, f.a1, y2));
+  const float q1mu = fmaf(d2, f.b2, d1 * f.b1);
+  const float q2mu2 = d2 * f.c2m;
   const float tau = sig * ds;
-  const float e = one_minus_exp(tau);
-  const float eps = 1.f - e;                          // exp(-tau)
-  const float R = fmaf(tau, tau - 2.f, 2.f * e * r3); // the reference's reuse term
-  const float Cc = fmaf(tau, fmaf(tau, tau - 3.f, 6.f), -6.f * e);
-  const float tme = tau - e;
-  // factors shared by the partials below
-  const float er1 = e * r1, epsds = eps * ds, tmer2 = tme * r2, cr4 = Cc * r4;
+  const float E = one_minus_exp(tau);
+  const float eps = 1.f - E;                          // exp(-tau)
+  const float T = (tau - E) * r2;
+  const float U = E * r1;
+  const float R = fmaf(2.f * E, r3, tau * (tau - 2.f));
+  const float C = fmaf(tau, fmaf(tau, tau - 3.f, 6.f), -6.f * E) * r4;
   AdjOut o;
-  o.pbar = fmaf(pbar, eps, abar * er1);
-  const float q0b = fmaf(abar, tmer2, pbar * er1);
-  const float q1b = mu * fmaf(abar, R, pbar * tmer2);
-  const float q2b = mu2 * fmaf(abar, cr4, pbar * R);
-  const float c1b = fmaf(q0b, zin, q1b);
-  const float c2b = fmaf(fmaf(q0b, zin, 2.f * q1b), zin, q2b);
-  o.y1b = c1b * a.rd1 + c2b * a.rd2;
-  o.y2b = q0b - 2.f * c2b * a.rd2;
-  o.y3b = c2b * a.rd2 - c1b * a.rd1;
-  o.c0b = q0b;                                        // q0 = c0 + c1 zin + c2 zin^2
-  o.c1b = c1b;
-  o.c2b = c2b;
-  // d/dsigma of the flux integral (A + q1 mu R + q2 mu^2 C/(3 sig^4)) and of the
-  // outgoing psi, with dtau/dsigma = ds and dE/dsigma = eps ds
-  const float sp = sig * psi - q0;
-  const float A = fmaf(q0, tau, sp * e) * r2;
-  const float dA = fmaf(fmaf(q0, ds, fmaf(psi, e, sp * epsds)), r2, -2.f * A * r1);
-  const float dR = fmaf(2.f * tau - 2.f, ds, r3 * fmaf(2.f, epsds, -6.f * er1));
-  const float dC = fmaf(fmaf(3.f * tau - 6.f, tau, 6.f), ds, -6.f * epsds);
-  const float q1mu = q1 * mu, q2mu2 = q2 * mu2;
-  const float dfi = fmaf(q1mu, dR, fmaf(q2mu2, fmaf(dC, r4, -4.f * cr4 * r1), dA));
-  const float dpn = fmaf(q0 * r1, epsds - er1,
-                         fmaf(q1mu, fmaf(e * ds, r2, -2.f * tme * r3), fmaf(q2mu2, dR, -psi * epsds)));
+  o.pbar = fmaf(pbar, eps, abar * U);
+  o.q0b = fmaf(abar, T, pbar * U);
+  o.q1mub = fmaf(abar, R, pbar * T);
+  o.q2mu2b = fmaf(abar, C, pbar * R);
+  // the fit, backwards: d1 = y1 - y3, d2 = y1 - 2 y2 + y3
+  const float d1b = fmaf(o.q0b, f.a1, o.q1mub * f.b1);
+  const float d2b = fmaf(o.q0b, f.a0, fmaf(o.q1mub, f.b2, o.q2mu2b * f.c2m));
+  o.y1b = d1b + d2b;
+  o.y2b = fmaf(-2.f, d2b, o.q0b);
+  o.y3b = d2b - d1b;
+  // sigma
+  const float Ep = ds * eps;
+  const float Up = (Ep - U) * r1;
+  const float Tp = fmaf(ds * E, r2, -2.f * T * r1);
+  const float Rp = fmaf(2.f * tau - 2.f, ds, 2.f * r3 * fmaf(-3.f, U, Ep));
+  const float Cp = fmaf(fmaf(fmaf(3.f, tau, -6.f), tau, 6.f) * ds - 6.f * Ep, r4, -4.f * C * r1);
+  const float dfi = fmaf(q0, Tp, fmaf(psi, Up, fmaf(q1mu, Rp, q2mu2 * Cp)));
+  const float dpn = fmaf(q0, Up, fmaf(q1mu, Tp, fmaf(q2mu2, Rp, -psi * Ep)));
   o.sbar = fmaf(abar, dfi, pbar * dpn);
   return o;
 }
@@ -1671,21 +1674,38 @@ __device__ __forceinline__ AdjOut adj_flat(float y, float sig, float r1, float d
   o.pbar = pbar + dbar * e;
   o.y1b = -dbar * e * r1;
   o.y2b = o.y3b = 0.f;
-  o.c0b = o.c1b = o.c2b = 0.f;
+  o.q0b = o.q1mub = o.q2mu2b = 0.f;
   o.sbar = dbar * (y * r1 * r1 * e + (psi - y * r1) * eps * ds);
   return o;
 }
 
-// The per-segment operands of one thread's chunks: sigma_t and 1/sigma_t, the
-// source rows and (reverse pass) dL/dphi of the tally row.
+// The per-segment operands of one thread's chunks.  The recomputation needs the
+// forward's coefficient planes and the fit rows; the reverse pass sigma_t,
+// 1/sigma_t, the fit rows and dL/dphi of the tally row.
 template <int CPL, bool QUAD>
-struct AdjRows {
-  float4 sig[CPL], r1[CPL], r2[CPL], r3x2[CPL], r4[CPL], y[CPL][QUAD ? 3 : 1], lam[CPL];
+struct AdjFwdRows {
+  float4 sig[CPL], r1[CPL], r2[CPL], r3x2[CPL], r4[CPL], y[CPL][QUAD ? 3 : 1];
+};
+template <int CPL, bool QUAD>
+struct AdjRevRows {
+  float4 sig[CPL], r1[CPL], y[CPL][QUAD ? 3 : 1], lam[CPL];
 };
 
-template <int CPL, bool QUAD, bool LAM>
-__device__ __forceinline__ void adj_load(const SweepArgs &a, const AdjArgs &x, const Seg &g,
-                                         int li, int TPW, AdjRows<CPL, QUAD> &r) {
+// the fit rows of one chunk, allocating in L1: the reverse pass reads the rows
+// the recomputation read a few segments before
+template <bool QUAD>
+__device__ __forceinline__ void adj_rows(const SweepArgs &a, const Seg &g, int c, float4 *y) {
+  const float *qr = a.q + g.qrow + 4 * c;
+  ld_row_vec<true>(qr, y[0]);
+  if (QUAD) {
+    ld_row_vec<true>(qr + a.ldg, y[QUAD ? 1 : 0]);
+    ld_row_vec<true>(qr + 2 * a.ldg, y[QUAD ? 2 : 0]);
+  }
+}
+
+template <int CPL, bool QUAD>
+__device__ __forceinline__ void adj_load_fwd(const SweepArgs &a, const Seg &g, int li, int TPW,
+                                             AdjFwdRows<CPL, QUAD> &r) {
 #pragma unroll
   for (int k = 0; k < CPL; ++k) {
     const int c = li + TPW * k;
@@ -1693,20 +1713,27 @@ __device__ __forceinline__ void adj_load(const SweepArgs &a, const AdjArgs &x, c
     const float *cf = a.coef + g.crow + 4 * COEF_PLANES * c;
     r.sig[k] = __ldg(reinterpret_cast<const float4 *>(cf));
     r.r1[k] = __ldg(reinterpret_cast<const float4 *>(cf + 4));
-    if (QUAD) {                         // the forward's planes, in both passes
+    if (QUAD) {
       r.r2[k] = __ldg(reinterpret_cast<const float4 *>(cf + 8));
       r.r4[k] = __ldg(reinterpret_cast<const float4 *>(cf + 16));
       r.r3x2[k] = __ldg(reinterpret_cast<const float4 *>(cf + 20));
     }
-    // the rows allocate in L1: the reverse pass reads the rows the
-    // recomputation read a few segments before
-    const float *qr = a.q + g.qrow + 4 * c;
-    ld_row_vec<true>(qr, r.y[k][0]);
-    if (QUAD) {
-      ld_row_vec<true>(qr + a.ldg, r.y[k][QUAD ? 1 : 0]);
-      ld_row_vec<true>(qr + 2 * a.ldg, r.y[k][QUAD ? 2 : 0]);
-    }
-    if (LAM) r.lam[k] = __ldg(reinterpret_cast<const float4 *>(x.dphi + g.frow + 4 * c));
+    adj_rows<QUAD>(a, g, c, r.y[k]);
+  }
+}
+
+template <int CPL, bool QUAD>
+__device__ __forceinline__ void adj_load_rev(const SweepArgs &a, const AdjArgs &x, const Seg &g,
+                                             int li, int TPW, AdjRevRows<CPL, QUAD> &r) {
+#pragma unroll
+  for (int k = 0; k < CPL; ++k) {
+    const int c = li + TPW * k;
+    if (c >= a.nchunk) continue;
+    const float *cf = a.coef + g.crow + 4 * COEF_PLANES * c;
+    r.sig[k] = __ldg(reinterpret_cast<const float4 *>(cf));
+    r.r1[k] = __ldg(reinterpret_cast<const float4 *>(cf + 4));
+    adj_rows<QUAD>(a, g, c, r.y[k]);
+    r.lam[k] = __ldg(reinterpret_cast<const float4 *>(x.dphi + g.frow + 4 * c));
   }
 }
 
@@ -1722,7 +1749,8 @@ constexpr size_t adj_hist_bytes() {
 // of nchunk float4 chunks takes exactly ceil(nchunk / CPL) lanes and a warp
 // holds floor(32 / width) tracks (G = 40: 10 lanes, three tracks a warp).  The
 // lanes left over run the loops with no chunk so that the warp stays converged.
-template <int CPL, bool QUAD>
+// FIT: dL/d of the quadratic fits' coefficients too (x.dfit).
+template <int CPL, bool QUAD, bool FIT = false>
 __global__ void __launch_bounds__(BLOCK, 2) adjoint_kernel(AdjArgs x) {
   extern __shared__ float4 s_adj[];
   const SweepArgs &a = x.a;
@@ -1781,111 +1809,147 @@ __global__ void __launch_bounds__(BLOCK, 2) adjoint_kernel(AdjArgs x) {
       // ---- recompute psi entering each segment of the block.  The loops over
       // the block stay rolled (unrolled, the derivative code outgrows the
       // instruction cache); each iteration issues the next segment's loads
-      // before its own arithmetic.
+      // before its own arithmetic (software pipeline, as the forward sweep).
       float z = a.ck_z[tr * NCK + b];
       float ds = __ldg(dsb + n0);
       Seg g = segment_geometry<true>(a, z, checked_source(a, __ldg(srcb + n0), li));
-      AdjRows<CPL, QUAD> cur;
+      // (one chunk a lane; with two the second set of operands would spill)
+      constexpr bool PF = CPL == 1;
+      {
+        AdjFwdRows<CPL, QUAD> cur;
+        if (PF) adj_load_fwd<CPL, QUAD>(a, g, li, TPW, cur);
 #pragma unroll 1
-      for (int jj = 0; jj < cnt; ++jj) {
-        if (li == 0) {
-          s_geo[jj] = g;
-          s_ds[jj] = ds;
-        }
-        adj_load<CPL, QUAD, false>(a, x, g, li, TPW, cur);
-        const MixedFit fit = QUAD ? mixed_fit(a, g.zin, mu, mu2) : MixedFit{};
-#pragma unroll
-        for (int k = 0; k < CPL; ++k) {
-          hist_base[(jj * CPL + k) * BLOCK] = psi[k];
-          const int c = li + TPW * k;
-          if (c >= a.nchunk) continue;
-#pragma unroll
-          for (int e = 0; e < 4; ++e) {
-            float p = get(psi[k], e);
-            if (QUAD)
-              mixed_quad(get(cur.y[k][0], e), get(cur.y[k][QUAD ? 1 : 0], e),
-                         get(cur.y[k][QUAD ? 2 : 0], e), fit, get(cur.sig[k], e),
-                         get(cur.r1[k], e), get(cur.r2[k], e), get(cur.r3x2[k], e),
-                         get(cur.r4[k], e), ds, w, p);
-            else
-              mixed_flat(get(cur.y[k][0], e), get(cur.sig[k], e), get(cur.r1[k], e), ds, w_mu, p);
-            set(psi[k], e, p);
+        for (int jj = 0; jj < cnt; ++jj) {
+          if (li == 0) {
+            s_geo[jj] = g;
+            s_ds[jj] = ds;
           }
-        }
-        if (jj + 1 < cnt) {
-          z = advance_z(a, z, ds, mu);
-          ds = __ldg(dsb + n0 + jj + 1);
-          g = segment_geometry<true>(a, z, checked_source(a, __ldg(srcb + n0 + jj + 1), li));
+          if (!PF) adj_load_fwd<CPL, QUAD>(a, g, li, TPW, cur);
+          float ds1 = ds;
+          Seg g1 = g;
+          AdjFwdRows<CPL, QUAD> nxt = cur;
+          if (jj + 1 < cnt) {
+            z = advance_z(a, z, ds, mu);
+            ds1 = __ldg(dsb + n0 + jj + 1);
+            g1 = segment_geometry<true>(a, z, checked_source(a, __ldg(srcb + n0 + jj + 1), li));
+            if (PF) adj_load_fwd<CPL, QUAD>(a, g1, li, TPW, nxt);
+          }
+          const MixedFit fit = QUAD ? mixed_fit(a, g.zin, mu, mu2) : MixedFit{};
+#pragma unroll
+          for (int k = 0; k < CPL; ++k) {
+            hist_base[(jj * CPL + k) * BLOCK] = psi[k];
+            const int c = li + TPW * k;
+            if (c >= a.nchunk) continue;
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+              float p = get(psi[k], e);
+              if (QUAD)
+                mixed_quad(get(cur.y[k][0], e), get(cur.y[k][QUAD ? 1 : 0], e),
+                           get(cur.y[k][QUAD ? 2 : 0], e), fit, get(cur.sig[k], e),
+                           get(cur.r1[k], e), get(cur.r2[k], e), get(cur.r3x2[k], e),
+                           get(cur.r4[k], e), ds, w, p);
+              else
+                mixed_flat(get(cur.y[k][0], e), get(cur.sig[k], e), get(cur.r1[k], e), ds, w_mu,
+                           p);
+              set(psi[k], e, p);
+            }
+          }
+          g = g1;
+          ds = ds1;
+          if (PF) cur = nxt;
         }
       }
       __syncwarp();
-      // ---- reverse through the block
+      // ---- reverse through the block, the previous segment's loads issued
+      // before this one's arithmetic
+      {
+        Seg gc = s_geo[cnt - 1];
+        float dsc = s_ds[cnt - 1];
+        AdjRevRows<CPL, QUAD> cur;
+        if (PF) adj_load_rev<CPL, QUAD>(a, x, gc, li, TPW, cur);
 #pragma unroll 1
-      for (int jj = cnt - 1; jj >= 0; --jj) {
-        g = s_geo[jj];
-        ds = s_ds[jj];
-        adj_load<CPL, QUAD, true>(a, x, g, li, TPW, cur);
-        const int mat = g.mat;
-#pragma unroll
-        for (int k = 0; k < CPL; ++k) {
-          const int c = li + TPW * k;
-          if (c >= a.nchunk) continue;
-          const int g4 = 4 * c;
-          const float4 ph = hist_base[(jj * CPL + k) * BLOCK];
-          float4 b1, b2, b3, sb, f0, f1, f2;
-#pragma unroll
-          for (int e = 0; e < 4; ++e) {
-            const float abar = get(cur.lam[k], e) * (QUAD ? w : w_mu);
-            const AdjOut o =
-                QUAD ? adj_quad(a, get(cur.y[k][0], e), get(cur.y[k][QUAD ? 1 : 0], e),
-                                get(cur.y[k][QUAD ? 2 : 0], e), get(cur.sig[k], e),
-                                get(cur.r1[k], e), get(cur.r2[k], e), get(cur.r3x2[k], e),
-                                get(cur.r4[k], e), g.zin, ds, mu, mu2, get(ph, e),
-                                get(pbar[k], e), abar)
-                     : adj_flat(get(cur.y[k][0], e), get(cur.sig[k], e), get(cur.r1[k], e), ds,
-                                get(ph, e), get(pbar[k], e), abar);
-            set(pbar[k], e, o.pbar);
-            set(b1, e, o.y1b);
-            set(b2, e, o.y2b);
-            set(b3, e, o.y3b);
-            set(sb, e, g4 + e < a.G ? o.sbar : 0.f);
-            set(f0, e, o.c0b);
-            set(f1, e, o.c1b);
-            set(f2, e, o.c2b);
+        for (int jj = cnt - 1; jj >= 0; --jj) {
+          if (!PF) adj_load_rev<CPL, QUAD>(a, x, gc, li, TPW, cur);
+          Seg gn = gc;
+          float dsn = dsc;
+          AdjRevRows<CPL, QUAD> nxt = cur;
+          if (jj > 0) {
+            gn = s_geo[jj - 1];
+            dsn = s_ds[jj - 1];
+            if (PF) adj_load_rev<CPL, QUAD>(a, x, gn, li, TPW, nxt);
           }
-          if (valid) {
-            if (acc) {
-              // one 16-byte read-modify-write per lane: the lanes of a
-              // sub-warp own distinct chunks of the row, sub-warps own slices
-              float4 *t = reinterpret_cast<float4 *>(acc + (int64_t)mat * a.ldg + g4);
-              float4 v = *t;
-              v.x += sb.x;
-              v.y += sb.y;
-              v.z += sb.z;
-              v.w += sb.w;
-              *t = v;
-            } else {
+          const int mat = gc.mat;
+          const MixedFit fit = QUAD ? mixed_fit(a, gc.zin, mu, mu2) : MixedFit{};
 #pragma unroll
-              for (int e = 0; e < 4; ++e)
-                if (g4 + e < a.G)
-                  atomicAdd(x.dsig + (int64_t)mat * a.ldg + g4 + e, (double)get(sb, e));
+          for (int k = 0; k < CPL; ++k) {
+            const int c = li + TPW * k;
+            if (c >= a.nchunk) continue;
+            const int g4 = 4 * c;
+            const float4 ph = hist_base[(jj * CPL + k) * BLOCK];
+            float4 b1, b2, b3, sb, f0, f1, f2;
+            vzero(f0);
+            vzero(f1);
+            vzero(f2);
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+              const float abar = get(cur.lam[k], e) * (QUAD ? w : w_mu);
+              const AdjOut o =
+                  QUAD ? adj_quad(get(cur.y[k][0], e), get(cur.y[k][QUAD ? 1 : 0], e),
+                                  get(cur.y[k][QUAD ? 2 : 0], e), fit, get(cur.sig[k], e),
+                                  get(cur.r1[k], e), dsc, get(ph, e), get(pbar[k], e), abar)
+                       : adj_flat(get(cur.y[k][0], e), get(cur.sig[k], e), get(cur.r1[k], e),
+                                  dsc, get(ph, e), get(pbar[k], e), abar);
+              set(pbar[k], e, o.pbar);
+              set(b1, e, o.y1b);
+              set(b2, e, o.y2b);
+              set(b3, e, o.y3b);
+              set(sb, e, g4 + e < a.G ? o.sbar : 0.f);
+              if (FIT) {
+                // dL/d of the fit's c0, c1, c2 (q0 = c0 + c1 zin + c2 zin^2,
+                // q1 = c1 + 2 c2 zin, q2 = c2)
+                const float q1b = mu * o.q1mub, q2b = mu2 * o.q2mu2b;
+                set(f0, e, o.q0b);
+                set(f1, e, fmaf(o.q0b, gc.zin, q1b));
+                set(f2, e, fmaf(fmaf(o.q0b, gc.zin, 2.f * q1b), gc.zin, q2b));
+              }
             }
-            float *dq = x.dq + g.qrow + g4;
-            red_add_v4(dq, b1.x, b1.y, b1.z, b1.w);
-            if (QUAD) {
-              red_add_v4(dq + a.ldg, b2.x, b2.y, b2.z, b2.w);
-              red_add_v4(dq + 2 * a.ldg, b3.x, b3.y, b3.z, b3.w);
-              if (x.dfit) {
-                // the fit window: its first row r0 of source s (rows s F + r0 ..)
-                const int64_t wrow = g.qrow / a.ldg;
-                const int64_t src = wrow / a.F, r0 = wrow - src * a.F;
-                float *df = x.dfit + ((src * (a.F - 2) + r0) * 3) * a.ldg + g4;
-                red_add_v4(df, f0.x, f0.y, f0.z, f0.w);
-                red_add_v4(df + a.ldg, f1.x, f1.y, f1.z, f1.w);
-                red_add_v4(df + 2 * a.ldg, f2.x, f2.y, f2.z, f2.w);
+            if (valid) {
+              if (acc) {
+                // one 16-byte read-modify-write per lane: the lanes of a
+                // sub-warp own distinct chunks of the row, sub-warps own slices
+                float4 *t = reinterpret_cast<float4 *>(acc + (int64_t)mat * a.ldg + g4);
+                float4 v = *t;
+                v.x += sb.x;
+                v.y += sb.y;
+                v.z += sb.z;
+                v.w += sb.w;
+                *t = v;
+              } else {
+#pragma unroll
+                for (int e = 0; e < 4; ++e)
+                  if (g4 + e < a.G)
+                    atomicAdd(x.dsig + (int64_t)mat * a.ldg + g4 + e, (double)get(sb, e));
+              }
+              float *dq = x.dq + gc.qrow + g4;
+              red_add_v4(dq, b1.x, b1.y, b1.z, b1.w);
+              if (QUAD) {
+                red_add_v4(dq + a.ldg, b2.x, b2.y, b2.z, b2.w);
+                red_add_v4(dq + 2 * a.ldg, b3.x, b3.y, b3.z, b3.w);
+                if (FIT) {
+                  // the fit window: its first row r0 of source s (rows s F + r0 ..)
+                  const int64_t wrow = gc.qrow / a.ldg;
+                  const int64_t src = wrow / a.F, r0 = wrow - src * a.F;
+                  float *df = x.dfit + ((src * (a.F - 2) + r0) * 3) * a.ldg + g4;
+                  red_add_v4(df, f0.x, f0.y, f0.z, f0.w);
+                  red_add_v4(df + a.ldg, f1.x, f1.y, f1.z, f1.w);
+                  red_add_v4(df + 2 * a.ldg, f2.x, f2.y, f2.z, f2.w);
+                }
               }
             }
           }
+          gc = gn;
+          dsc = dsn;
+          if (PF) cur = nxt;
         }
       }
       __syncwarp();
@@ -1912,7 +1976,7 @@ __global__ void __launch_bounds__(BLOCK, 2) adjoint_kernel(AdjArgs x) {
 
 template <int CPL, bool QUAD>
 int launch_adj_t(moc_problem *p, const AdjArgs &x, int tpw) {
-  auto kern = adjoint_kernel<CPL, QUAD>;
+  auto kern = x.dfit ? adjoint_kernel<CPL, QUAD, true> : adjoint_kernel<CPL, QUAD, false>;
   AdjArgs y = x;
   y.tpw = tpw;
   y.nsub = (BLOCK / 32) * (32 / tpw);
