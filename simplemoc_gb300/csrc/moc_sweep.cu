@@ -311,9 +311,9 @@ __device__ __forceinline__ MixedFit mixed_fit(const SweepArgs &a, float zin, flo
 // reuse term R = tau (tau - 2) + 2E/sig^3 (its precedence kept, as PLAIN).
 // r1, r2, r3x2, r4 are the coefficient planes 1/sig, 1/sig^2, 2/sig^3,
 // 1/(3 sig^4).
-__device__ __forceinline__ float mixed_quad(float y1, float y2, float y3, const MixedFit &f,
-                                            float sig, float r1, float r2, float r3x2,
-                                            float r4, float ds, float w, float &p) {
+__device__ __forceinline__ float mixed_quad_e(float y1, float y2, float y3, const MixedFit &f,
+                                              float sig, float r1, float r2, float r3x2,
+                                              float r4, float ds, float w, float &p, float &Eo) {
   const float d1 = y1 - y3;
   const float d2 = fmaf(-2.f, y2, y1) + y3;
   const float q0 = fmaf(d2, f.a0, fmaf(d1, f.a1, y2));
@@ -327,7 +327,17 @@ __device__ __forceinline__ float mixed_quad(float y1, float y2, float y3, const 
   const float Cr = fmaf(tau, fmaf(tau, tau - 3.f, 6.f), -6.f * E) * r4;
   const float fi = fmaf(q0, T, fmaf(p, U, fmaf(q1mu, R, q2mu2 * Cr)));
   p = fmaf(q0, U, fmaf(q1mu, T, fmaf(q2mu2, R, p * (1.f - E))));
+  Eo = E;
   return w * fi;
+}
+
+// (mixed_quad_e also gives E = 1 - e^-tau, which the adjoint's recomputation
+// keeps for the reverse pass)
+__device__ __forceinline__ float mixed_quad(float y1, float y2, float y3, const MixedFit &f,
+                                            float sig, float r1, float r2, float r3x2,
+                                            float r4, float ds, float w, float &p) {
+  float E;
+  return mixed_quad_e(y1, y2, y3, f, sig, r1, r2, r3x2, r4, ds, w, p, E);
 }
 
 __device__ __forceinline__ float mixed_flat(float y, float sig, float r1, float ds, float w_mu,
@@ -1627,8 +1637,8 @@ struct AdjOut {
 //   U' = (E' - U)/sig, T' = ds E/sig^2 - 2T/sig, R' = (2tau - 2) ds + 2/sig^3 (E' - 3U),
 //   C' = ((3tau^2 - 6tau + 6) ds - 6E')/(3 sig^4) - 4C/sig.
 __device__ __forceinline__ AdjOut adj_quad(float y1, float y2, float y3, const MixedFit &f,
-                                           float sig, float r1, float ds, float psi, float pbar,
-                                           float abar) {
+                                           float sig, float r1, float ds, float E, float psi,
+                                           float pbar, float abar) {
   const float r2 = r1 * r1, r3 = r1 * r2, r4 = r2 * r2 * (1.0f / 3.0f);
   const float d1 = y1 - y3;
   const float d2 = fmaf(-2.f, y2, y1) + y3;
@@ -1636,8 +1646,7 @@ __device__ __forceinline__ AdjOut adj_quad(float y1, float y2, float y3, const M
   const float q1mu = fmaf(d2, f.b2, d1 * f.b1);
   const float q2mu2 = d2 * f.c2m;
   const float tau = sig * ds;
-  const float E = one_minus_exp(tau);
-  const float eps = 1.f - E;                          // exp(-tau)
+  const float eps = 1.f - E;                          // exp(-tau); E from the recomputation
   const float T = (tau - E) * r2;
   const float U = E * r1;
   const float R = fmaf(2.f * E, r3, tau * (tau - 2.f));
@@ -1740,9 +1749,11 @@ __device__ __forceinline__ void adj_load_rev(const SweepArgs &a, const AdjArgs &
 // Shared memory of the reverse sweep: the recomputed angular flux of the
 // current checkpoint block (ADJ_KMAX x CPL float4 per thread), then the
 // per-sub-warp dL/dsigma_t accumulators when they fit.
+// Two planes per thread and block segment: psi entering it and (quadratic
+// source) E = 1 - e^-tau of its groups, both from the recomputation.
 template <int CPL>
 constexpr size_t adj_hist_bytes() {
-  return sizeof(float4) * (size_t)BLOCK * ADJ_KMAX * CPL;
+  return 2 * sizeof(float4) * (size_t)BLOCK * ADJ_KMAX * CPL;
 }
 
 // Lanes per track are a runtime width: the kernel has no shuffles, so a track
@@ -1763,9 +1774,10 @@ __global__ void __launch_bounds__(BLOCK, 2) adjoint_kernel(AdjArgs x) {
   const int sub = (threadIdx.x >> 5) * GPW + gw;
   // this thread's history slots: hist(jj, k) at s_adj[(jj * CPL + k) * BLOCK + threadIdx.x]
   float4 *hist_base = s_adj + threadIdx.x;
+  float4 *ehist_base = hist_base + (size_t)BLOCK * ADJ_KMAX * CPL;
   // the block's segment geometry and lengths, one copy per track (written by
   // its lane 0)
-  Seg *s_geo_all = reinterpret_cast<Seg *>(s_adj + (size_t)BLOCK * ADJ_KMAX * CPL);
+  Seg *s_geo_all = reinterpret_cast<Seg *>(s_adj + (size_t)2 * BLOCK * ADJ_KMAX * CPL);
   Seg *s_geo = s_geo_all + (size_t)sub * ADJ_KMAX;
   float *s_ds_all = reinterpret_cast<float *>(s_geo_all + (size_t)x.nsub * ADJ_KMAX);
   float *s_ds = s_ds_all + (size_t)sub * ADJ_KMAX;
@@ -1840,19 +1852,23 @@ __global__ void __launch_bounds__(BLOCK, 2) adjoint_kernel(AdjArgs x) {
             hist_base[(jj * CPL + k) * BLOCK] = psi[k];
             const int c = li + TPW * k;
             if (c >= a.nchunk) continue;
+            float4 ev;
 #pragma unroll
             for (int e = 0; e < 4; ++e) {
               float p = get(psi[k], e);
+              float Ee = 0.f;
               if (QUAD)
-                mixed_quad(get(cur.y[k][0], e), get(cur.y[k][QUAD ? 1 : 0], e),
-                           get(cur.y[k][QUAD ? 2 : 0], e), fit, get(cur.sig[k], e),
-                           get(cur.r1[k], e), get(cur.r2[k], e), get(cur.r3x2[k], e),
-                           get(cur.r4[k], e), ds, w, p);
+                mixed_quad_e(get(cur.y[k][0], e), get(cur.y[k][QUAD ? 1 : 0], e),
+                             get(cur.y[k][QUAD ? 2 : 0], e), fit, get(cur.sig[k], e),
+                             get(cur.r1[k], e), get(cur.r2[k], e), get(cur.r3x2[k], e),
+                             get(cur.r4[k], e), ds, w, p, Ee);
               else
                 mixed_flat(get(cur.y[k][0], e), get(cur.sig[k], e), get(cur.r1[k], e), ds, w_mu,
                            p);
               set(psi[k], e, p);
+              set(ev, e, Ee);
             }
+            if (QUAD) ehist_base[(jj * CPL + k) * BLOCK] = ev;
           }
           g = g1;
           ds = ds1;
@@ -1886,6 +1902,7 @@ __global__ void __launch_bounds__(BLOCK, 2) adjoint_kernel(AdjArgs x) {
             if (c >= a.nchunk) continue;
             const int g4 = 4 * c;
             const float4 ph = hist_base[(jj * CPL + k) * BLOCK];
+            const float4 eh = QUAD ? ehist_base[(jj * CPL + k) * BLOCK] : ph;
             float4 b1, b2, b3, sb, f0, f1, f2;
             vzero(f0);
             vzero(f1);
@@ -1896,7 +1913,8 @@ __global__ void __launch_bounds__(BLOCK, 2) adjoint_kernel(AdjArgs x) {
               const AdjOut o =
                   QUAD ? adj_quad(get(cur.y[k][0], e), get(cur.y[k][QUAD ? 1 : 0], e),
                                   get(cur.y[k][QUAD ? 2 : 0], e), fit, get(cur.sig[k], e),
-                                  get(cur.r1[k], e), dsc, get(ph, e), get(pbar[k], e), abar)
+                                  get(cur.r1[k], e), dsc, get(eh, e), get(ph, e),
+                                  get(pbar[k], e), abar)
                        : adj_flat(get(cur.y[k][0], e), get(cur.sig[k], e), get(cur.r1[k], e),
                                   dsc, get(ph, e), get(pbar[k], e), abar);
               set(pbar[k], e, o.pbar);
