@@ -405,7 +405,10 @@ def run_adjoint(args):
     """The adjoint workload: the small problem's geometry with 40 groups, one
     fixed-source sweep and its reverse sweep (psi checkpoints every 8
     segments).  Reports forward, forward-with-checkpoints and reverse times
-    (events on the library stream, via the C ABI) and their ratio."""
+    (events on the library stream, via the C ABI).  value = reverse / forward:
+    the checkpointed forward replaces the plain forward at the same cost, so the
+    gradient costs the reverse sweep; (checkpointed forward + reverse) / forward
+    is reported beside it."""
     import ctypes as C
 
     import torch
@@ -434,7 +437,8 @@ def run_adjoint(args):
                 rv.append(rms.value)
     f, r = float(np.median(fw)), float(np.median(rv))
     line = {
-        "metric": "adjoint sweep time / forward sweep time", "value": (f + r) / t_fwd,
+        "metric": "adjoint (reverse) sweep time / forward sweep time", "value": r / t_fwd,
+        "checkpointed_forward_plus_reverse_over_forward": (f + r) / t_fwd,
         "unit": "ratio", "n_gpus": 1, "steps": K, "warmup": W, "higher_is_better": False,
         "dtype": "f32", "data": "synthetic (seeded)",
         "config": {"workload": f"adjoint: {spec.n_tracks_3d} tracks x {spec.n_seg} segments x "
