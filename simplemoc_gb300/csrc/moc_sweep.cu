@@ -331,14 +331,6 @@ __device__ __forceinline__ float mixed_quad_e(float y1, float y2, float y3, cons
   return w * fi;
 }
 
-// (mixed_quad_e also gives E = 1 - e^-tau, which the adjoint's recomputation
-// keeps for the reverse pass)
-__device__ __forceinline__ float mixed_quad(float y1, float y2, float y3, const MixedFit &f,
-                                            float sig, float r1, float r2, float r3x2,
-                                            float r4, float ds, float w, float &p) {
-  float E;
-  return mixed_quad_e(y1, y2, y3, f, sig, r1, r2, r3x2, r4, ds, w, p, E);
-}
 
 __device__ __forceinline__ float mixed_flat(float y, float sig, float r1, float ds, float w_mu,
                                             float &p) {
@@ -346,6 +338,81 @@ __device__ __forceinline__ float mixed_flat(float y, float sig, float r1, float 
   float dpsi = (p - y * r1) * e;
   p -= dpsi;
   return w_mu * dpsi;
+}
+
+// ---- packed pairs of groups.  sm_100 and later issue one FP32 FMA, multiply
+// or add on two lanes at once (__ffma2_rn, __fmul2_rn, __fadd2_rn), each lane
+// rounded as __fmaf_rn / __fmul_rn / __fadd_rn (a - b is written fma(b, -1, a):
+// one rounding of the same difference).  Pairs halve the instructions but also
+// the independent chains a thread has in flight, so they pay only where issue
+// slots, not latency, bound a loop (the adjoint's reverse pass).
+__device__ __forceinline__ float2 bc2(float v) { return make_float2(v, v); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 lo2(const float4 &v) { return make_float2(v.x, v.y); }
+__device__ __forceinline__ float2 hi2(const float4 &v) { return make_float2(v.z, v.w); }
+__device__ __forceinline__ float4 cat4(float2 l, float2 h) { return make_float4(l.x, l.y, h.x, h.y); }
+
+// MixedFit with every factor on both lanes
+struct MixedFit2 {
+  float2 a1, a0, b1, b2, c2m;
+};
+__device__ __forceinline__ MixedFit2 pair_fit(const MixedFit &f) {
+  return MixedFit2{bc2(f.a1), bc2(f.a0), bc2(f.b1), bc2(f.b2), bc2(f.c2m)};
+}
+
+// one_minus_exp on two lanes
+__device__ __forceinline__ float2 one_minus_exp2(float2 t) {
+  float2 s = fma2(t, bc2(1.0f / 40320.0f), bc2(-1.0f / 5040.0f));
+  s = fma2(t, s, bc2(1.0f / 720.0f));
+  s = fma2(t, s, bc2(-1.0f / 120.0f));
+  s = fma2(t, s, bc2(1.0f / 24.0f));
+  s = fma2(t, s, bc2(-1.0f / 6.0f));
+  s = fma2(t, s, bc2(0.5f));
+  const float2 nt = mul2(t, bc2(-1.0f));
+  s = fma2(nt, s, bc2(1.0f));                 // 1 - t s
+  const float2 small = mul2(t, s);
+  return make_float2(t.x < 0.5f ? small.x : 1.0f - __expf(nt.x),
+                     t.y < 0.5f ? small.y : 1.0f - __expf(nt.y));
+}
+
+// mixed_quad_e's tally and psi on two groups, operation for operation: the
+// same bits (the sweeps run this; the adjoint's recomputation, which also
+// keeps E, runs mixed_quad_e)
+__device__ __forceinline__ float2 mixed_quad_v(float2 y1, float2 y2, float2 y3,
+                                               const MixedFit2 &f, float2 sig, float2 r1,
+                                               float2 r2, float2 r3x2, float2 r4, float2 ds,
+                                               float2 w, float2 &p) {
+  const float2 m1 = bc2(-1.f);
+  const float2 d1 = fma2(y3, m1, y1);
+  const float2 d2 = add2(fma2(bc2(-2.f), y2, y1), y3);
+  const float2 q0 = fma2(d2, f.a0, fma2(d1, f.a1, y2));
+  const float2 q1mu = fma2(d2, f.b2, mul2(d1, f.b1));
+  const float2 q2mu2 = mul2(d2, f.c2m);
+  const float2 tau = mul2(sig, ds);
+  const float2 E = one_minus_exp2(tau);
+  const float2 T = mul2(fma2(E, m1, tau), r2);
+  const float2 U = mul2(E, r1);
+  const float2 R = fma2(E, r3x2, mul2(tau, add2(tau, bc2(-2.f))));
+  const float2 Cr =
+      mul2(fma2(tau, fma2(tau, add2(tau, bc2(-3.f)), bc2(6.f)), mul2(bc2(-6.f), E)), r4);
+  const float2 fi = fma2(q0, T, fma2(p, U, fma2(q1mu, R, mul2(q2mu2, Cr))));
+  p = fma2(q0, U, fma2(q1mu, T, fma2(q2mu2, R, mul2(p, fma2(E, m1, bc2(1.f))))));
+  return mul2(w, fi);
+}
+// four groups as two pairs
+__device__ __forceinline__ float4 mixed_quad_v(float4 y1, float4 y2, float4 y3,
+                                               const MixedFit2 &f, float4 sig, float4 r1,
+                                               float4 r2, float4 r3x2, float4 r4, float2 ds,
+                                               float2 w, float4 &p) {
+  float2 pl = lo2(p), ph = hi2(p);
+  const float2 tl = mixed_quad_v(lo2(y1), lo2(y2), lo2(y3), f, lo2(sig), lo2(r1), lo2(r2),
+                                 lo2(r3x2), lo2(r4), ds, w, pl);
+  const float2 th = mixed_quad_v(hi2(y1), hi2(y2), hi2(y3), f, hi2(sig), hi2(r1), hi2(r2),
+                                 hi2(r3x2), hi2(r4), ds, w, ph);
+  p = cat4(pl, ph);
+  return cat4(tl, th);
 }
 
 // The rounding error of old + x (TwoSum, Knuth): exact in round-to-nearest.
@@ -573,6 +640,7 @@ __device__ __forceinline__ void sweep_track(const SweepArgs &a, int64_t track, i
     }
     // ---- segment n
     const MixedFit fit = (MODE == MODE_MIXED && QUAD) ? mixed_fit(a, g.zin, mu, mu2) : MixedFit{};
+    const MixedFit2 fit2 = pair_fit(fit);
 #pragma unroll
     for (int k = 0; k < CPL; ++k) {
       const int c = li + TPW * k;
@@ -612,13 +680,8 @@ __device__ __forceinline__ void sweep_track(const SweepArgs &a, int64_t track, i
           ldg_vec(cf + 8, r2);
           ldg_vec(cf + 16, r4);
           ldg_vec(cf + 20, r3x2);
-#pragma unroll
-          for (int e = 0; e < VW; ++e) {
-            float p = get(psi[k], e);
-            set(t, e, mixed_quad(get(y1, e), get(y2, e), get(y3, e), fit, get(sig, e), get(r1, e),
-                                 get(r2, e), get(r3x2, e), get(r4, e), ds, w, p));
-            set(psi[k], e, p);
-          }
+          // groups in packed pairs: mixed_quad_e's bits
+          t = mixed_quad_v(y1, y2, y3, fit2, sig, r1, r2, r3x2, r4, bc2(ds), bc2(w), psi[k]);
         }
       } else {
         const V y = rows.v[k][0];
@@ -954,13 +1017,8 @@ __global__ void __launch_bounds__(BLOCK) sweep_staged_kernel(SweepArgs a, int ro
             const float4 r2 = __ldg(reinterpret_cast<const float4 *>(cf + 8));
             const float4 r4 = __ldg(reinterpret_cast<const float4 *>(cf + 16));
             const float4 r3x2 = __ldg(reinterpret_cast<const float4 *>(cf + 20));
-#pragma unroll
-            for (int e = 0; e < 4; ++e) {
-              float p = get(psi[k], e);
-              set(t, e, mixed_quad(get(y1, e), get(y2, e), get(y3, e), fit, get(sig, e),
-                                   get(r1, e), get(r2, e), get(r3x2, e), get(r4, e), ds, w, p));
-              set(psi[k], e, p);
-            }
+            t = mixed_quad_v(y1, y2, y3, pair_fit(fit), sig, r1, r2, r3x2, r4, bc2(ds), bc2(w),
+                             psi[k]);
           }
         } else {
 #pragma unroll
@@ -1625,7 +1683,7 @@ struct AdjOut {
   float q0b, q1mub, q2mu2b;   // quadratic source: dL/d q0, d(q1 mu), d(q2 mu^2)
 };
 
-// Reverse of mixed_quad for one group.  With the per-segment fit factors f
+// Reverse of mixed_quad_e for one group.  With the per-segment fit factors f
 // (mixed_fit), E = 1 - e^-tau and the weights
 //   T = (tau - E)/sig^2, U = E/sig, R = tau (tau - 2) + 2E/sig^3 (the reference's
 //   reuse term), C = (tau^3 - 3 tau^2 + 6 tau - 6E)/(3 sig^4),
@@ -1636,41 +1694,48 @@ struct AdjOut {
 // (tau = sig ds, E' = ds (1 - E)):
 //   U' = (E' - U)/sig, T' = ds E/sig^2 - 2T/sig, R' = (2tau - 2) ds + 2/sig^3 (E' - 3U),
 //   C' = ((3tau^2 - 6tau + 6) ds - 6E')/(3 sig^4) - 4C/sig.
-__device__ __forceinline__ AdjOut adj_quad(float y1, float y2, float y3, const MixedFit &f,
-                                           float sig, float r1, float ds, float E, float psi,
-                                           float pbar, float abar) {
-  const float r2 = r1 * r1, r3 = r1 * r2, r4 = r2 * r2 * (1.0f / 3.0f);
-  const float d1 = y1 - y3;
-  const float d2 = fmaf(-2.f, y2, y1) + y3;
-  const float q0 = fmaf(d2, f.a0, fmaf(d1, f.a1, y2));
-  const float q1mu = fmaf(d2, f.b2, d1 * f.b1);
-  const float q2mu2 = d2 * f.c2m;
-  const float tau = sig * ds;
-  const float eps = 1.f - E;                          // exp(-tau); E from the recomputation
-  const float T = (tau - E) * r2;
-  const float U = E * r1;
-  const float R = fmaf(2.f * E, r3, tau * (tau - 2.f));
-  const float C = fmaf(tau, fmaf(tau, tau - 3.f, 6.f), -6.f * E) * r4;
-  AdjOut o;
-  o.pbar = fmaf(pbar, eps, abar * U);
-  o.q0b = fmaf(abar, T, pbar * U);
-  o.q1mub = fmaf(abar, R, pbar * T);
-  o.q2mu2b = fmaf(abar, C, pbar * R);
-  // the fit, backwards: d1 = y1 - y3, d2 = y1 - 2 y2 + y3
-  const float d1b = fmaf(o.q0b, f.a1, o.q1mub * f.b1);
-  const float d2b = fmaf(o.q0b, f.a0, fmaf(o.q1mub, f.b2, o.q2mu2b * f.c2m));
-  o.y1b = d1b + d2b;
-  o.y2b = fmaf(-2.f, d2b, o.q0b);
-  o.y3b = d2b - d1b;
-  // sigma
-  const float Ep = ds * eps;
-  const float Up = (Ep - U) * r1;
-  const float Tp = fmaf(ds * E, r2, -2.f * T * r1);
-  const float Rp = fmaf(2.f * tau - 2.f, ds, 2.f * r3 * fmaf(-3.f, U, Ep));
-  const float Cp = fmaf(fmaf(fmaf(3.f, tau, -6.f), tau, 6.f) * ds - 6.f * Ep, r4, -4.f * C * r1);
-  const float dfi = fmaf(q0, Tp, fmaf(psi, Up, fmaf(q1mu, Rp, q2mu2 * Cp)));
-  const float dpn = fmaf(q0, Up, fmaf(q1mu, Tp, fmaf(q2mu2, Rp, -psi * Ep)));
-  o.sbar = fmaf(abar, dfi, pbar * dpn);
+// Two groups at once, on packed FP32 pairs.
+struct AdjOut2 {
+  float2 pbar, y1b, y2b, y3b, sbar, q0b, q1mub, q2mu2b;
+};
+__device__ __forceinline__ AdjOut2 adj_quad2(float2 y1, float2 y2, float2 y3, const MixedFit2 &f,
+                                             float2 sig, float2 r1, float2 ds, float2 E,
+                                             float2 psi, float2 pbar, float2 abar) {
+  const float2 m1 = bc2(-1.f), two = bc2(2.f);
+  const float2 r2 = mul2(r1, r1), r3 = mul2(r1, r2);
+  const float2 r4 = mul2(mul2(r2, r2), bc2(1.0f / 3.0f));
+  const float2 d1 = fma2(y3, m1, y1);
+  const float2 d2 = add2(fma2(bc2(-2.f), y2, y1), y3);
+  const float2 q0 = fma2(d2, f.a0, fma2(d1, f.a1, y2));
+  const float2 q1mu = fma2(d2, f.b2, mul2(d1, f.b1));
+  const float2 q2mu2 = mul2(d2, f.c2m);
+  const float2 tau = mul2(sig, ds);
+  const float2 eps = fma2(E, m1, bc2(1.f));
+  const float2 T = mul2(fma2(E, m1, tau), r2);
+  const float2 U = mul2(E, r1);
+  const float2 R = fma2(mul2(two, E), r3, mul2(tau, add2(tau, bc2(-2.f))));
+  const float2 C =
+      mul2(fma2(tau, fma2(tau, add2(tau, bc2(-3.f)), bc2(6.f)), mul2(bc2(-6.f), E)), r4);
+  AdjOut2 o;
+  o.pbar = fma2(pbar, eps, mul2(abar, U));
+  o.q0b = fma2(abar, T, mul2(pbar, U));
+  o.q1mub = fma2(abar, R, mul2(pbar, T));
+  o.q2mu2b = fma2(abar, C, mul2(pbar, R));
+  const float2 d1b = fma2(o.q0b, f.a1, mul2(o.q1mub, f.b1));
+  const float2 d2b = fma2(o.q0b, f.a0, fma2(o.q1mub, f.b2, mul2(o.q2mu2b, f.c2m)));
+  o.y1b = add2(d1b, d2b);
+  o.y2b = fma2(bc2(-2.f), d2b, o.q0b);
+  o.y3b = fma2(d1b, m1, d2b);
+  const float2 Ep = mul2(ds, eps);
+  const float2 Up = mul2(fma2(U, m1, Ep), r1);
+  const float2 Tp = fma2(mul2(ds, E), r2, mul2(mul2(bc2(-2.f), T), r1));
+  const float2 Rp = fma2(fma2(two, tau, bc2(-2.f)), ds, mul2(mul2(two, r3), fma2(bc2(-3.f), U, Ep)));
+  const float2 Cp = fma2(fma2(fma2(fma2(bc2(3.f), tau, bc2(-6.f)), tau, bc2(6.f)), ds,
+                              mul2(bc2(-6.f), Ep)),
+                         r4, mul2(mul2(bc2(-4.f), C), r1));
+  const float2 dfi = fma2(q0, Tp, fma2(psi, Up, fma2(q1mu, Rp, mul2(q2mu2, Cp))));
+  const float2 dpn = fma2(q0, Up, fma2(q1mu, Tp, fma2(q2mu2, Rp, mul2(mul2(psi, m1), Ep))));
+  o.sbar = fma2(abar, dfi, mul2(pbar, dpn));
   return o;
 }
 
@@ -1895,7 +1960,8 @@ __global__ void __launch_bounds__(BLOCK, 2) adjoint_kernel(AdjArgs x) {
             if (PF) adj_load_rev<CPL, QUAD>(a, x, gn, li, TPW, nxt);
           }
           const int mat = gc.mat;
-          const MixedFit fit = QUAD ? mixed_fit(a, gc.zin, mu, mu2) : MixedFit{};
+          const MixedFit2 fit2 = pair_fit(QUAD ? mixed_fit(a, gc.zin, mu, mu2) : MixedFit{});
+          const float2 ds2 = bc2(dsc);
 #pragma unroll
           for (int k = 0; k < CPL; ++k) {
             const int c = li + TPW * k;
@@ -1907,28 +1973,56 @@ __global__ void __launch_bounds__(BLOCK, 2) adjoint_kernel(AdjArgs x) {
             vzero(f0);
             vzero(f1);
             vzero(f2);
+            if (QUAD) {
+              // groups in pairs
+              float2 pb[2], y1b[2], y2b[2], y3b[2], sbr[2], c0b[2], c1b[2], c2b[2];
 #pragma unroll
-            for (int e = 0; e < 4; ++e) {
-              const float abar = get(cur.lam[k], e) * (QUAD ? w : w_mu);
-              const AdjOut o =
-                  QUAD ? adj_quad(get(cur.y[k][0], e), get(cur.y[k][QUAD ? 1 : 0], e),
-                                  get(cur.y[k][QUAD ? 2 : 0], e), fit, get(cur.sig[k], e),
-                                  get(cur.r1[k], e), dsc, get(eh, e), get(ph, e),
-                                  get(pbar[k], e), abar)
-                       : adj_flat(get(cur.y[k][0], e), get(cur.sig[k], e), get(cur.r1[k], e),
-                                  dsc, get(ph, e), get(pbar[k], e), abar);
-              set(pbar[k], e, o.pbar);
-              set(b1, e, o.y1b);
-              set(b2, e, o.y2b);
-              set(b3, e, o.y3b);
-              set(sb, e, g4 + e < a.G ? o.sbar : 0.f);
+              for (int h = 0; h < 2; ++h) {
+                auto half = [h](const float4 &v) { return h ? hi2(v) : lo2(v); };
+                const AdjOut2 o =
+                    adj_quad2(half(cur.y[k][0]), half(cur.y[k][QUAD ? 1 : 0]),
+                              half(cur.y[k][QUAD ? 2 : 0]), fit2, half(cur.sig[k]),
+                              half(cur.r1[k]), ds2, half(eh), half(ph), half(pbar[k]),
+                              mul2(half(cur.lam[k]), bc2(w)));
+                pb[h] = o.pbar;
+                y1b[h] = o.y1b;
+                y2b[h] = o.y2b;
+                y3b[h] = o.y3b;
+                sbr[h] = o.sbar;
+                if (FIT) {
+                  // dL/d of the fit's c0, c1, c2 (q0 = c0 + c1 zin + c2 zin^2,
+                  // q1 = c1 + 2 c2 zin, q2 = c2)
+                  const float2 zin = bc2(gc.zin);
+                  const float2 q1b = mul2(bc2(mu), o.q1mub), q2b = mul2(bc2(mu2), o.q2mu2b);
+                  c0b[h] = o.q0b;
+                  c1b[h] = fma2(o.q0b, zin, q1b);
+                  c2b[h] = fma2(fma2(o.q0b, zin, mul2(bc2(2.f), q1b)), zin, q2b);
+                }
+              }
+              pbar[k] = cat4(pb[0], pb[1]);
+              b1 = cat4(y1b[0], y1b[1]);
+              b2 = cat4(y2b[0], y2b[1]);
+              b3 = cat4(y3b[0], y3b[1]);
+              sb = cat4(sbr[0], sbr[1]);
               if (FIT) {
-                // dL/d of the fit's c0, c1, c2 (q0 = c0 + c1 zin + c2 zin^2,
-                // q1 = c1 + 2 c2 zin, q2 = c2)
-                const float q1b = mu * o.q1mub, q2b = mu2 * o.q2mu2b;
-                set(f0, e, o.q0b);
-                set(f1, e, fmaf(o.q0b, gc.zin, q1b));
-                set(f2, e, fmaf(fmaf(o.q0b, gc.zin, 2.f * q1b), gc.zin, q2b));
+                f0 = cat4(c0b[0], c0b[1]);
+                f1 = cat4(c1b[0], c1b[1]);
+                f2 = cat4(c2b[0], c2b[1]);
+              }
+#pragma unroll
+              for (int e = 0; e < 4; ++e)
+                if (g4 + e >= a.G) set(sb, e, 0.f);
+            } else {
+#pragma unroll
+              for (int e = 0; e < 4; ++e) {
+                const AdjOut o = adj_flat(get(cur.y[k][0], e), get(cur.sig[k], e),
+                                          get(cur.r1[k], e), dsc, get(ph, e), get(pbar[k], e),
+                                          get(cur.lam[k], e) * w_mu);
+                set(pbar[k], e, o.pbar);
+                set(b1, e, o.y1b);
+                set(b2, e, o.y2b);
+                set(b3, e, o.y3b);
+                set(sb, e, g4 + e < a.G ? o.sbar : 0.f);
               }
             }
             if (valid) {

@@ -290,7 +290,7 @@ def test_update_sources_adjoint_vs_torch_fp64(gpu_available, G, F, n_mat):
         S2, N2 = S0.clone().requires_grad_(True), N0.clone().requires_grad_(True)
         q2 = fl.source_reference(p2, S2, N2).reshape(-1)
         (q2 * dq).sum().backward()
-    rel = lambda a, b: float((a - b).abs().max() / b.abs().max())
+    rel = lambda a, b: float((a - b).detach().abs().max() / b.detach().abs().max())
     assert rel(q1.double(), q2.detach()) <= 1e-6
     assert rel(S1.grad, S2.grad) <= 1e-6
     fuel = N2.grad.abs().amax(dim=1) > 0
