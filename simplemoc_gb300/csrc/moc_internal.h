@@ -58,6 +58,10 @@ struct SweepArgs {
   float dz, rdz;            // fine interval height and its reciprocal
   float d1, rd1, d2, rd2;   // 2 dz and 2 dz dz, and reciprocals
   float hd;                 // domain height
+  // 1, -1 and -0 as values the compiler cannot see: the PLAIN pair arithmetic
+  // multiplies and adds through FMAs with them, which it can neither simplify
+  // nor contract (the reference rounds every product and sum on its own)
+  float rt_one, rt_m1, rt_nz;
   uint32_t fmagic;          // zi % F == zi - F*umulhi(zi, fmagic) for reachable zi; 0 = use %
   int32_t *err;             // device error word (0 = ok)
   // psi checkpoints of the adjoint's forward sweep: every ck_k segments,

@@ -152,15 +152,6 @@ __device__ __forceinline__ void ldg_vec(const float *p, float2 &v) {
   v = __ldg(reinterpret_cast<const float2 *>(p));
 }
 
-// Reference interpolation table, src/solver.c:1441-1464.
-__device__ __forceinline__ float table_lookup(const SweepArgs &a, const float2 *tab, float x) {
-  if (x > a.table_maxval) return 1.0f;
-  int idx = __float2int_rz(__fadd_rn(div_cr(x, a.table_dx, a.table_rdx), a.table_halfdx));
-  idx = max(0, min(idx, a.table_n - 1));
-  float2 se = tab[idx];
-  return __fadd_rn(__fmul_rn(se.x, x), se.y);
-}
-
 // 1 - exp(-tau) to ~1e-7 relative: Taylor series below 0.5, SFU exponential above.
 __device__ __forceinline__ float one_minus_exp(float t) {
   // (1 - e^-t) / t = sum_k (-t)^k / (k+1)!, to degree 7: the first omitted
@@ -235,48 +226,6 @@ __device__ __forceinline__ float advance_z(const SweepArgs &a, float z, float ds
 #pragma unroll 1
   for (int it = 0; it < 4 && z < 0.0f; ++it) z = __fadd_rn(z, a.hd);
   return z;
-}
-
-// ---- PLAIN arithmetic for one group, quadratic source (src/solver.c:74-278)
-__device__ __forceinline__ float plain_quad(const SweepArgs &a, const float2 *tab, float y1,
-                                            float y2, float y3, float sig, float sig2,
-                                            float sig3, float sig4, float r1, float r2,
-                                            float r3, float r4, float zin, float ds,
-                                            float mu, float mu2, float w, float &p) {
-  float c0 = y2;
-  float c1 = div_cr(__fsub_rn(y1, y3), a.d1, a.rd1);
-  float c2 = div_cr(__fadd_rn(__fsub_rn(y1, __fmul_rn(2.f, y2)), y3), a.d2, a.rd2);
-  float q0 = __fadd_rn(__fadd_rn(c0, __fmul_rn(c1, zin)), __fmul_rn(__fmul_rn(c2, zin), zin));
-  float q1 = __fadd_rn(c1, __fmul_rn(__fmul_rn(2.f, c2), zin));
-  float q2 = c2;
-  float tau = __fmul_rn(sig, ds);
-  float e = table_lookup(a, tab, tau);
-  float reuse = __fadd_rn(__fmul_rn(tau, __fsub_rn(tau, 2.f)), div_cr(__fmul_rn(2.f, e), sig3, r3));
-  float A = div_cr(__fadd_rn(__fmul_rn(q0, tau), __fmul_rn(__fsub_rn(__fmul_rn(sig, p), q0), e)),
-                   sig2, r2);
-  float B = __fmul_rn(__fmul_rn(q1, mu), reuse);
-  float cub = __fsub_rn(__fmul_rn(tau, __fadd_rn(__fmul_rn(tau, __fsub_rn(tau, 3.f)), 6.f)),
-                        __fmul_rn(6.f, e));
-  float C = div_cr(__fmul_rn(__fmul_rn(q2, mu2), cub), sig4, r4);
-  float fi = __fadd_rn(__fadd_rn(A, B), C);
-  float t1 = div_cr(__fmul_rn(q0, e), sig, r1);
-  float t2 = div_cr(__fmul_rn(__fmul_rn(q1, mu), __fsub_rn(tau, e)), sig2, r2);
-  float t3 = __fmul_rn(__fmul_rn(q2, mu2), reuse);
-  float t4 = __fmul_rn(p, __fsub_rn(1.f, e));
-  p = __fadd_rn(__fadd_rn(__fadd_rn(t1, t2), t3), t4);
-  return __fmul_rn(w, fi);
-}
-
-// ---- PLAIN flat source (src/solver.c:1075-1115)
-__device__ __forceinline__ float plain_flat(const SweepArgs &a, const float2 *tab, float y,
-                                            float sig, float r1, float ds, float w_mu,
-                                            float &p) {
-  float tau = __fmul_rn(sig, ds);
-  float e = table_lookup(a, tab, tau);
-  float qq = div_cr(y, sig, r1);
-  float dpsi = __fmul_rn(__fsub_rn(p, qq), e);
-  p = __fsub_rn(p, dpsi);
-  return __fmul_rn(w_mu, dpsi);
 }
 
 // ---- MIXED arithmetic, quadratic source
@@ -360,6 +309,117 @@ struct MixedFit2 {
 };
 __device__ __forceinline__ MixedFit2 pair_fit(const MixedFit &f) {
   return MixedFit2{bc2(f.a1), bc2(f.a0), bc2(f.b1), bc2(f.b2), bc2(f.c2m)};
+}
+
+// ---- PLAIN: the reference's float arithmetic, operation for operation, on
+// two groups at once.  Each of its operations is one rounding, and the packed
+// pair FMA rounds each lane as __fmaf_rn, so every product, sum and difference
+// is an FMA with a runtime 1, -1 or -0 (RN(a b + -0) = RN(a b), RN(a 1 + b) =
+// RN(a + b), RN(b (-1) + a) = RN(a - b), signed zeros included).  Plain pair
+// multiplies and adds would be legal for the compiler to contract into one
+// FMA, which the reference never does.  A divisor enters div_cr only as -b in
+// fma(-q, b, a) = fma(q, -b, a), so the pair forms carry the negated divisors
+// (-sig, -sig^2, -sig^3, -3 sig^4, formed with the reference's roundings:
+// RN(-x) = -RN(x)).
+struct Exact2 {
+  float2 one, m1, nz;
+};
+__device__ __forceinline__ Exact2 exact2(const SweepArgs &a) {
+  return Exact2{bc2(a.rt_one), bc2(a.rt_m1), bc2(a.rt_nz)};
+}
+__device__ __forceinline__ float2 xmul(const Exact2 &k, float2 a, float2 b) { return fma2(a, b, k.nz); }
+__device__ __forceinline__ float2 xadd(const Exact2 &k, float2 a, float2 b) { return fma2(a, k.one, b); }
+__device__ __forceinline__ float2 xsub(const Exact2 &k, float2 a, float2 b) { return fma2(b, k.m1, a); }
+// div_cr on two lanes
+__device__ __forceinline__ float2 xdiv(const Exact2 &k, float2 a, float2 nb, float2 rb) {
+  const float2 q = xmul(k, a, rb);
+  return fma2(fma2(q, nb, a), rb, q);
+}
+
+// The reference's interpolation table (src/solver.c:1441-1464) on two lanes.
+__device__ __forceinline__ float2 table_lookup2(const SweepArgs &a, const Exact2 &k,
+                                                const float2 *tab, float2 x) {
+  const float2 f = xadd(k, xdiv(k, x, bc2(-a.table_dx), bc2(a.table_rdx)), bc2(a.table_halfdx));
+  const int i0 = max(0, min(__float2int_rz(f.x), a.table_n - 1));
+  const int i1 = max(0, min(__float2int_rz(f.y), a.table_n - 1));
+  const float2 s0 = tab[i0], s1 = tab[i1];
+  const float2 v = xadd(k, xmul(k, make_float2(s0.x, s1.x), x), make_float2(s0.y, s1.y));
+  return make_float2(x.x > a.table_maxval ? 1.0f : v.x, x.y > a.table_maxval ? 1.0f : v.y);
+}
+
+// quadratic source, src/solver.c:74-278
+__device__ __forceinline__ float2 plain_quad_v(const SweepArgs &a, const float2 *tab, float2 y1,
+                                               float2 y2, float2 y3, float2 sig, float2 r1,
+                                               float2 r2, float2 r3, float2 r4, float2 zin,
+                                               float2 ds, float2 mu, float2 mu2, float2 w,
+                                               float2 &p) {
+  const Exact2 k = exact2(a);
+  const float2 two = bc2(2.f);
+  // the reference's divisors (solver.c:153, 176, 198), negated
+  const float2 nsg = xmul(k, sig, k.m1);
+  const float2 nsg2 = xmul(k, nsg, sig);
+  const float2 nsg3 = xmul(k, sig, nsg2);
+  const float2 nsg4 = xmul(k, xmul(k, bc2(-3.f), nsg2), nsg2);
+  const float2 c0 = y2;
+  const float2 c1 = xdiv(k, xsub(k, y1, y3), bc2(-a.d1), bc2(a.rd1));
+  const float2 c2 =
+      xdiv(k, xadd(k, xsub(k, y1, xmul(k, two, y2)), y3), bc2(-a.d2), bc2(a.rd2));
+  const float2 q0 = xadd(k, xadd(k, c0, xmul(k, c1, zin)), xmul(k, xmul(k, c2, zin), zin));
+  const float2 q1 = xadd(k, c1, xmul(k, xmul(k, two, c2), zin));
+  const float2 q2 = c2;
+  const float2 tau = xmul(k, sig, ds);
+  const float2 e = table_lookup2(a, k, tab, tau);
+  const float2 reuse =
+      xadd(k, xmul(k, tau, xsub(k, tau, two)), xdiv(k, xmul(k, two, e), nsg3, r3));
+  const float2 A = xdiv(
+      k, xadd(k, xmul(k, q0, tau), xmul(k, xsub(k, xmul(k, sig, p), q0), e)), nsg2, r2);
+  const float2 q1mu = xmul(k, q1, mu);
+  const float2 B = xmul(k, q1mu, reuse);
+  const float2 cub = xsub(k, xmul(k, tau, xadd(k, xmul(k, tau, xsub(k, tau, bc2(3.f))), bc2(6.f))),
+                          xmul(k, bc2(6.f), e));
+  const float2 q2mu2 = xmul(k, q2, mu2);
+  const float2 C = xdiv(k, xmul(k, q2mu2, cub), nsg4, r4);
+  const float2 fi = xadd(k, xadd(k, A, B), C);
+  const float2 t1 = xdiv(k, xmul(k, q0, e), nsg, r1);
+  const float2 t2 = xdiv(k, xmul(k, q1mu, xsub(k, tau, e)), nsg2, r2);
+  const float2 t3 = xmul(k, q2mu2, reuse);
+  const float2 t4 = xmul(k, p, xsub(k, k.one, e));
+  p = xadd(k, xadd(k, xadd(k, t1, t2), t3), t4);
+  return xmul(k, w, fi);
+}
+__device__ __forceinline__ float4 plain_quad_v(const SweepArgs &a, const float2 *tab, float4 y1,
+                                               float4 y2, float4 y3, float4 sig, float4 r1,
+                                               float4 r2, float4 r3, float4 r4, float2 zin,
+                                               float2 ds, float2 mu, float2 mu2, float2 w,
+                                               float4 &p) {
+  float2 pl = lo2(p), ph = hi2(p);
+  const float2 tl = plain_quad_v(a, tab, lo2(y1), lo2(y2), lo2(y3), lo2(sig), lo2(r1), lo2(r2),
+                                 lo2(r3), lo2(r4), zin, ds, mu, mu2, w, pl);
+  const float2 th = plain_quad_v(a, tab, hi2(y1), hi2(y2), hi2(y3), hi2(sig), hi2(r1), hi2(r2),
+                                 hi2(r3), hi2(r4), zin, ds, mu, mu2, w, ph);
+  p = cat4(pl, ph);
+  return cat4(tl, th);
+}
+
+// flat source, src/solver.c:1075-1115
+__device__ __forceinline__ float2 plain_flat_v(const SweepArgs &a, const float2 *tab, float2 y,
+                                               float2 sig, float2 r1, float2 ds, float2 w_mu,
+                                               float2 &p) {
+  const Exact2 k = exact2(a);
+  const float2 e = table_lookup2(a, k, tab, xmul(k, sig, ds));
+  const float2 qq = xdiv(k, y, xmul(k, sig, k.m1), r1);
+  const float2 dpsi = xmul(k, xsub(k, p, qq), e);
+  p = xsub(k, p, dpsi);
+  return xmul(k, w_mu, dpsi);
+}
+__device__ __forceinline__ float4 plain_flat_v(const SweepArgs &a, const float2 *tab, float4 y,
+                                               float4 sig, float4 r1, float2 ds, float2 w_mu,
+                                               float4 &p) {
+  float2 pl = lo2(p), ph = hi2(p);
+  const float2 tl = plain_flat_v(a, tab, lo2(y), lo2(sig), lo2(r1), ds, w_mu, pl);
+  const float2 th = plain_flat_v(a, tab, hi2(y), hi2(sig), hi2(r1), ds, w_mu, ph);
+  p = cat4(pl, ph);
+  return cat4(tl, th);
 }
 
 // one_minus_exp on two lanes
@@ -662,19 +722,9 @@ __device__ __forceinline__ void sweep_track(const SweepArgs &a, int64_t track, i
           ldg_vec(cf + 8, r2);
           ldg_vec(cf + 12, r3);
           ldg_vec(cf + 16, r4);
-#pragma unroll
-          for (int e = 0; e < VW; ++e) {
-            // the reference's divisors, formed with its own operations
-            const float sg = get(sig, e);
-            const float sg2 = __fmul_rn(sg, sg);                        // solver.c:153
-            const float sg3 = __fmul_rn(sg, sg2);                       // solver.c:176
-            const float sg4 = __fmul_rn(__fmul_rn(3.f, sg2), sg2);      // solver.c:198
-            float p = get(psi[k], e);
-            set(t, e, plain_quad(a, s_table, get(y1, e), get(y2, e), get(y3, e), sg, sg2, sg3,
-                                 sg4, get(r1, e), get(r2, e), get(r3, e), get(r4, e), g.zin,
-                                 ds, mu, mu2, w, p));
-            set(psi[k], e, p);
-          }
+          // groups in packed pairs, the reference's roundings
+          t = plain_quad_v(a, s_table, y1, y2, y3, sig, r1, r2, r3, r4, bc2(g.zin), bc2(ds),
+                           bc2(mu), bc2(mu2), bc2(w), psi[k]);
         } else {
           V r2, r4, r3x2;
           ldg_vec(cf + 8, r2);
@@ -685,14 +735,15 @@ __device__ __forceinline__ void sweep_track(const SweepArgs &a, int64_t track, i
         }
       } else {
         const V y = rows.v[k][0];
+        if (MODE == MODE_PLAIN) {
+          t = plain_flat_v(a, s_table, y, sig, r1, bc2(ds), bc2(w_mu), psi[k]);
+        } else {
 #pragma unroll
-        for (int e = 0; e < VW; ++e) {
-          float p = get(psi[k], e);
-          if (MODE == MODE_PLAIN)
-            set(t, e, plain_flat(a, s_table, get(y, e), get(sig, e), get(r1, e), ds, w_mu, p));
-          else
+          for (int e = 0; e < VW; ++e) {
+            float p = get(psi[k], e);
             set(t, e, mixed_flat(get(y, e), get(sig, e), get(r1, e), ds, w_mu, p));
-          set(psi[k], e, p);
+            set(psi[k], e, p);
+          }
         }
       }
       if (REC) {
@@ -1001,18 +1052,8 @@ __global__ void __launch_bounds__(BLOCK) sweep_staged_kernel(SweepArgs a, int ro
             const float4 r2 = __ldg(reinterpret_cast<const float4 *>(cf + 8));
             const float4 r3 = __ldg(reinterpret_cast<const float4 *>(cf + 12));
             const float4 r4 = __ldg(reinterpret_cast<const float4 *>(cf + 16));
-#pragma unroll
-            for (int e = 0; e < 4; ++e) {
-              const float sgm = get(sig, e);
-              const float sg2 = __fmul_rn(sgm, sgm);                      // solver.c:153
-              const float sg3 = __fmul_rn(sgm, sg2);                      // solver.c:176
-              const float sg4 = __fmul_rn(__fmul_rn(3.f, sg2), sg2);      // solver.c:198
-              float p = get(psi[k], e);
-              set(t, e, plain_quad(a, s_table, get(y1, e), get(y2, e), get(y3, e), sgm, sg2, sg3,
-                                   sg4, get(r1, e), get(r2, e), get(r3, e), get(r4, e), sg.zin,
-                                   ds, mu, mu2, w, p));
-              set(psi[k], e, p);
-            }
+            t = plain_quad_v(a, s_table, y1, y2, y3, sig, r1, r2, r3, r4, bc2(sg.zin), bc2(ds),
+                             bc2(mu), bc2(mu2), bc2(w), psi[k]);
           } else {
             const float4 r2 = __ldg(reinterpret_cast<const float4 *>(cf + 8));
             const float4 r4 = __ldg(reinterpret_cast<const float4 *>(cf + 16));
@@ -1021,14 +1062,15 @@ __global__ void __launch_bounds__(BLOCK) sweep_staged_kernel(SweepArgs a, int ro
                              psi[k]);
           }
         } else {
+          if (MODE == MODE_PLAIN) {
+            t = plain_flat_v(a, s_table, y1, sig, r1, bc2(ds), bc2(w_mu), psi[k]);
+          } else {
 #pragma unroll
-          for (int e = 0; e < 4; ++e) {
-            float p = get(psi[k], e);
-            if (MODE == MODE_PLAIN)
-              set(t, e, plain_flat(a, s_table, get(y1, e), get(sig, e), get(r1, e), ds, w_mu, p));
-            else
+            for (int e = 0; e < 4; ++e) {
+              float p = get(psi[k], e);
               set(t, e, mixed_flat(get(y1, e), get(sig, e), get(r1, e), ds, w_mu, p));
-            set(psi[k], e, p);
+              set(psi[k], e, p);
+            }
           }
         }
         if (valid) {
@@ -1378,6 +1420,9 @@ SweepArgs build_args(moc_problem *p) {
   a.table_rdx = 1.0f / d.table_dx;
   a.table_halfdx = 0.5f * d.table_dx;
   a.table_maxval = d.table_maxval;
+  a.rt_one = 1.0f;
+  a.rt_m1 = -1.0f;
+  a.rt_nz = -0.0f;
   // src/solver.c:38 -- float height over the int product
   a.dz = d.height / (float)(d.fai * d.decomp_ax * d.cai);
   a.rdz = 1.0f / a.dz;
