@@ -65,6 +65,8 @@ def _args():
     ap.add_argument("--accuracy-iters", type=int, default=20,
                     help="power iterations of the accuracy comparison against the FP64 mode "
                          "(on the whole workload)")
+    ap.add_argument("--floor", action="store_true",
+                    help="accuracy: also FP64 arithmetic on FP32-rounded state")
     ap.add_argument("--no-compensated", action="store_true",
                     help="skip timing MIXED with compensated tallies")
     ap.add_argument("--launch", default=None, metavar="TPW,CPL",
@@ -262,10 +264,12 @@ def flux_errors(a, ref, G: int) -> dict:
     }
 
 
-def accuracy_block(spec, device: int, iters: int) -> dict:
+def accuracy_block(spec, device: int, iters: int, floor: bool = False) -> dict:
     """Every mode against the FP64 mode (the same formulas in double with an
     exact 1 - exp(-tau)) on the whole workload over `iters` power iterations:
-    FSR flux errors normwise, per FSR and per element, and the k_eff error."""
+    FSR flux errors normwise, per FSR and per element, and the k_eff error.
+    floor: also FP64 arithmetic on state rounded to FP32 after every step
+    (MOC_FLAG_FP32_STATE), the error that FP32 storage alone sets."""
     import simplemoc_gb300 as sm
     hp = sm.generate(spec, with_state=False)
     t0 = time.perf_counter()
@@ -286,6 +290,13 @@ def accuracy_block(spec, device: int, iters: int) -> dict:
         e["normwise_within_contract"] = (e["normwise"] <= CONTRACT
                                          and e["keff_rel_err"] <= KEFF_CONTRACT)
         out[name] = e
+    if floor:
+        with sm.Solver(hp, device=device, mode="fp64", fp32_state=True) as s:
+            h = s.run(iters)
+            ph = s.download64(fine_flux=True)["fine_flux"]
+        e = flux_errors(ph, p64, spec.n_groups)
+        e["keff_rel_err"] = abs(h[-1][0] - k64) / abs(k64)
+        out["fp64_on_fp32_state"] = e
     return out
 
 
@@ -658,7 +669,7 @@ def main():
     accuracy = None
     if not args.no_accuracy and rank == 0:
         solver.close()                  # room for the FP64 state
-        accuracy = accuracy_block(spec, local, max(1, args.accuracy_iters))
+        accuracy = accuracy_block(spec, local, max(1, args.accuracy_iters), args.floor)
 
     # ---- CPU baseline (rank 0, N = 1 only) -------------------------------------
     cpu = None
