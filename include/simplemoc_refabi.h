@@ -158,9 +158,17 @@ int moc_ref_status(void);
 /* Sub-segments of the last sweep (Input.segments_processed). */
 int64_t moc_ref_last_segments(void);
 /* Host milliseconds the last sweep spent drawing its rand() values
- * (MOC_REF_RNG_LIBC: one libc rand() per sub-segment on the calling thread,
- * the serial reference's sequence; 0 in the hash mode). */
+ * (MOC_REF_RNG_LIBC: one libc rand() value per sub-segment on the calling
+ * thread, the serial reference's sequence; 0 in the hash mode). */
 double moc_ref_last_rng_ms(void);
+/* The draws of MOC_REF_RNG_LIBC: the next n values of the process's rand()
+ * sequence into out, libc's state left as n rand() calls leave it.  With
+ * glibc's additive generator states (the default one included) they are
+ * produced in bulk from the generator's state (*bulk = 1, after a one-time
+ * check against rand() itself); otherwise by n rand() calls (*bulk = 0).  No
+ * other thread may call rand() meanwhile, as in the serial reference.
+ * MOC_ERR_ARG for n < 0 or a NULL out with n > 0; bulk may be NULL. */
+int moc_ref_libc_draws(int32_t *out, int64_t n, int *bulk);
 
 #ifdef __cplusplus
 }

@@ -26,7 +26,7 @@ ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 CU_SOURCES = ["moc_api.cu", "moc_sweep.cu", "moc_post.cu", "moc_refabi.cu", "moc_batch.cu",
               "moc_update_tc.cu", "moc_determ.cu", "moc_update_adj.cu"]
-CPP_SOURCES = ["moc_host.cpp", "moc_openmoc.cpp"]
+CPP_SOURCES = ["moc_host.cpp", "moc_openmoc.cpp", "moc_libc_rand.cpp"]
 
 
 def _nvcc() -> str:

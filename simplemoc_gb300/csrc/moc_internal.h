@@ -76,6 +76,11 @@ struct SweepArgs {
   const int32_t *csr_src;   // [M] source regions
 };
 
+// The next n values of the process's libc rand() sequence, libc's state
+// advanced as by n calls (moc_libc_rand.cpp).  Returns 1 if they were drawn in
+// bulk from libc's generator state, 0 if by n rand() calls.
+int moc_libc_draws(int32_t *out, int64_t n);
+
 struct MocDet;   // deterministic-order tally buffers (moc_determ.cu)
 
 struct moc_problem {

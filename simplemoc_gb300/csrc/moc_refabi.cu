@@ -341,7 +341,8 @@ struct RefState {
   int64_t *d_ij_tot = nullptr, *d_ij_base = nullptr, *d_off = nullptr;
   float *d_sds = nullptr, *d_sz = nullptr;
   int32_t *d_ssrc = nullptr, *d_rng = nullptr;
-  int64_t cap = 0;
+  int32_t *h_rng = nullptr;       // pinned staging of the rand() draws
+  int64_t cap = 0, h_rng_cap = 0;
   int64_t sweeps = 0;
   int64_t last_segments = 0;
   double last_rng_ms = 0.0;
@@ -365,6 +366,7 @@ void release_ref() {
   dfree(r.d_seg_off); dfree(r.d_seg_len); dfree(r.d_cos); dfree(r.d_sin); dfree(r.d_z);
   dfree(r.d_zc); dfree(r.d_cnt); dfree(r.d_ij_tot); dfree(r.d_ij_base); dfree(r.d_off);
   dfree(r.d_sds); dfree(r.d_sz); dfree(r.d_ssrc); dfree(r.d_rng);
+  if (r.h_rng) cudaFreeHost(r.h_rng);
   r = RefState();
 }
 
@@ -598,13 +600,21 @@ int sweep_ref(int64_t *segments) {
   r.last_rng_ms = 0.0;
   if (g_rng_mode == MOC_REF_RNG_LIBC && M > 0) {
     // the serial reference draws rand() once per sub-segment in traversal
-    // order (src/solver.c:481); the same draws, from the process's libc state
+    // order (src/solver.c:481); the same draws, from the process's libc state,
+    // in bulk where libc's generator allows it (moc_libc_rand.cpp)
+    if (M > r.h_rng_cap) {
+      if (r.h_rng) cudaFreeHost(r.h_rng);
+      r.h_rng = nullptr;
+      r.h_rng_cap = 0;
+      const int64_t cap = M + M / 8 + 1024;
+      MOC_CUDA_TRY(cudaMallocHost(&r.h_rng, sizeof(int32_t) * (size_t)cap));
+      r.h_rng_cap = cap;
+    }
     const auto t0 = std::chrono::steady_clock::now();
-    std::vector<int32_t> rv((size_t)M);
-    for (int64_t k = 0; k < M; ++k) rv[(size_t)k] = rand();
+    moc_libc_draws(r.h_rng, M);
     r.last_rng_ms =
         std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-    MOC_CUDA_TRY(cudaMemcpyAsync(r.d_rng, rv.data(), sizeof(int32_t) * (size_t)M,
+    MOC_CUDA_TRY(cudaMemcpyAsync(r.d_rng, r.h_rng, sizeof(int32_t) * (size_t)M,
                                  cudaMemcpyHostToDevice, st));
     MOC_CUDA_TRY(cudaStreamSynchronize(st));
   }
@@ -741,5 +751,12 @@ int moc_ref_status(void) { return g_status; }
 int64_t moc_ref_last_segments(void) { return g_ref.last_segments; }
 
 double moc_ref_last_rng_ms(void) { return g_ref.last_rng_ms; }
+
+int moc_ref_libc_draws(int32_t *out, int64_t n, int *bulk) {
+  if (n < 0 || (n > 0 && !out)) return MOC_ERR_ARG;
+  const int b = moc_libc_draws(out, n);
+  if (bulk) *bulk = b;
+  return MOC_OK;
+}
 
 }  // extern "C"

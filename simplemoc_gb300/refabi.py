@@ -100,6 +100,8 @@ def lib() -> C.CDLL:
         lb.moc_ref_last_segments.restype = C.c_int64
         lb.moc_ref_last_rng_ms.argtypes = []
         lb.moc_ref_last_rng_ms.restype = C.c_double
+        lb.moc_ref_libc_draws.argtypes = [C.POINTER(C.c_int32), C.c_int64, C.POINTER(C.c_int)]
+        lb.moc_ref_libc_draws.restype = C.c_int
         _BOUND = True
     return lb
 

@@ -180,4 +180,4 @@ def test_reference_entry_points_match_the_drop_in_header(lib):
         seen += 1
         if got != want:
             bad.append((name, want, got))
-    assert seen == 10 and not bad, (seen, bad)
+    assert seen == 11 and not bad, (seen, bad)
