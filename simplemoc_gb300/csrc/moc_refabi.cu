@@ -152,10 +152,13 @@ __device__ __forceinline__ void stage_put(const RefArgs &r, float *buf, int64_t 
 // EMIT: the sub-segments go to slots slot, slot + 1, ... of the streams, through
 // the ray's staging group `stg` (the ray's stream starts at slot `first`) or,
 // with stg null, directly.
-template <bool EMIT>
+// KEEP (counting call of the emitting pass): the first KEEP sub-segments'
+// (ds, height) also go to keep[], so that the emitting call can be skipped.
+template <bool EMIT, int KEEP = 0>
 __device__ int track_segment(const RefArgs &r, bool pos, double cos_d, float s_full, float &zh,
                              bool last_seg, int k, bool *hit, int64_t slot, int64_t seq,
-                             float *stg = nullptr, int64_t first = 0) {
+                             float *stg = nullptr, int64_t first = 0,
+                             float2 *keep = nullptr) {
   float s = s_full;
   // get_pos_interval / get_neg_interval (src/solver.c:895-907): float z / dz
   int curr = pos ? __float2int_rz(__fdiv_rn(zh, r.fine_dz_f))
@@ -189,6 +192,7 @@ __device__ int track_segment(const RefArgs &r, bool pos, double cos_d, float s_f
         *hit = true;
       }
     }
+    if (KEEP > 0 && count < KEEP) keep[count] = make_float2(ds, zh);
     if (EMIT) {
       const int32_t src = sub_segment_source(r, seq + count);
       if (stg) {
@@ -216,6 +220,10 @@ __device__ __forceinline__ int warp_incl_scan(int v, int lane) {
   }
   return v;
 }
+
+// Sub-segments of one ray over one 2D segment that the emitting pass keeps from
+// its counting call (about one on average; more are evaluated again).
+constexpr int REF_KEEP = 4;
 
 // STAGED (pass 1): the warp's stacked rays keep their staging groups in
 // dynamic shared memory, 24 words per ray, Z rays per warp.
@@ -261,9 +269,13 @@ __global__ void __launch_bounds__(128) ref_expand(RefArgs r) {
       bool hit = false;
       int c = 0;
       float zh = 0.f;
+      // pass 1: the sub-segments of this call, emitted below without a second
+      // evaluation of the double-precision split when they all fit
+      float2 keep[PASS == 1 ? REF_KEEP : 1];
       if (active) {
         zh = zst[k];
-        c = track_segment<false>(r, pos, cos_d, s_full, zh, last_seg, k, &hit, 0, 0);
+        c = track_segment<false, PASS == 1 ? REF_KEEP : 0>(r, pos, cos_d, s_full, zh, last_seg,
+                                                           k, &hit, 0, 0, nullptr, 0, keep);
       }
       const unsigned amask = __ballot_sync(FULL, active);
       const unsigned H = __ballot_sync(FULL, active && hit);
@@ -289,13 +301,29 @@ __global__ void __launch_bounds__(128) ref_expand(RefArgs r) {
           zst[k] = zh;
           cst[k] += c;
         } else {
-          float zz = zst[k];
-          bool h2;
           const int64_t t = ij * r.Z + k;
-          track_segment<true>(r, pos, cos_d, s_full, zz, last_seg, k, &h2,
-                              r.off[t] + cst[k], r.ij_base[ij] + local + (incl - cm),
-                              STAGED ? wstage + (size_t)k * 24 : nullptr, r.off[t]);
-          zst[k] = zz;
+          const int64_t first = r.off[t], slot = first + cst[k];
+          const int64_t seq = r.ij_base[ij] + local + (incl - cm);
+          float *stg = STAGED ? wstage + (size_t)k * 24 : nullptr;
+          if (c <= REF_KEEP) {
+            for (int q = 0; q < c; ++q) {
+              const int32_t src = sub_segment_source(r, seq + q);
+              if (stg) {
+                stage_put(r, stg, first, slot + q, keep[q].x, keep[q].y, src);
+              } else {
+                r.sds[slot + q] = keep[q].x;
+                r.sz[slot + q] = keep[q].y;
+                r.ssrc[slot + q] = src;
+              }
+            }
+            zst[k] = zh;
+          } else {
+            float zz = zst[k];
+            bool h2;
+            track_segment<true>(r, pos, cos_d, s_full, zz, last_seg, k, &h2, slot, seq, stg,
+                                first);
+            zst[k] = zz;
+          }
           cst[k] += c;
         }
       }
