@@ -104,33 +104,38 @@ __device__ __forceinline__ int32_t sub_segment_source(const RefArgs &r, int64_t 
 // Staged stores of the emitting pass.  Each lane writes the sub-segments of a
 // different stacked ray, so direct 4-byte stores scatter over as many sectors
 // as lanes; partly written sectors then cost a read and a write each in DRAM.
-// Instead each ray's entries collect in an 8-entry group in shared memory
-// (ds, z, source: 24 words) and leave as whole 32-byte sectors of each stream
-// once the group is full.  A ray's first and last groups are shared with the
-// neighbouring rays' streams and go out entry by entry.
+// Instead each ray's entries collect in a STAGE_N-entry group in shared memory
+// (ds, z, source: 3 STAGE_N words) and leave as whole 16-byte pieces of each
+// stream once the group is full; the two pieces of a 32-byte sector meet in L2.
+// A ray's first and last groups are shared with the neighbouring rays' streams
+// and go out entry by entry.
+constexpr int STAGE_N = 4;
+constexpr int STAGE_W = 3 * STAGE_N;     // words per ray
+
 // Writes the entries [max(g0, first), end) of the group that ends at `end`
-// (g0 = the group's first slot, a multiple of 8).
+// (g0 = the group's first slot, a multiple of STAGE_N).
 __device__ __forceinline__ void stage_flush(const RefArgs &r, const float *buf, int64_t first,
                                             int64_t end) {
-  const int64_t g0 = (end - 1) & ~int64_t(7);
-  const int32_t *bsrc = reinterpret_cast<const int32_t *>(buf + 16);
-  if (g0 >= first && end - g0 == 8) {
-    // whole group: the streams are 256-byte aligned, so slot g0 starts a sector
+  const int64_t g0 = (end - 1) & ~int64_t(STAGE_N - 1);
+  const int32_t *bsrc = reinterpret_cast<const int32_t *>(buf + 2 * STAGE_N);
+  if (g0 >= first && end - g0 == STAGE_N) {
+    // whole group: the streams are 256-byte aligned, so slot g0 starts a 16-byte piece
     float4 *ds4 = reinterpret_cast<float4 *>(r.sds + g0);
     float4 *z4 = reinterpret_cast<float4 *>(r.sz + g0);
     int4 *s4 = reinterpret_cast<int4 *>(r.ssrc + g0);
-    ds4[0] = make_float4(buf[0], buf[1], buf[2], buf[3]);
-    ds4[1] = make_float4(buf[4], buf[5], buf[6], buf[7]);
-    z4[0] = make_float4(buf[8], buf[9], buf[10], buf[11]);
-    z4[1] = make_float4(buf[12], buf[13], buf[14], buf[15]);
-    s4[0] = make_int4(bsrc[0], bsrc[1], bsrc[2], bsrc[3]);
-    s4[1] = make_int4(bsrc[4], bsrc[5], bsrc[6], bsrc[7]);
+#pragma unroll
+    for (int v = 0; v < STAGE_N / 4; ++v) {
+      ds4[v] = make_float4(buf[4 * v], buf[4 * v + 1], buf[4 * v + 2], buf[4 * v + 3]);
+      z4[v] = make_float4(buf[STAGE_N + 4 * v], buf[STAGE_N + 4 * v + 1],
+                          buf[STAGE_N + 4 * v + 2], buf[STAGE_N + 4 * v + 3]);
+      s4[v] = make_int4(bsrc[4 * v], bsrc[4 * v + 1], bsrc[4 * v + 2], bsrc[4 * v + 3]);
+    }
     return;
   }
   for (int64_t x = g0 > first ? g0 : first; x < end; ++x) {
     const int e = (int)(x - g0);
     r.sds[x] = buf[e];
-    r.sz[x] = buf[8 + e];
+    r.sz[x] = buf[STAGE_N + e];
     r.ssrc[x] = bsrc[e];
   }
 }
@@ -139,11 +144,11 @@ __device__ __forceinline__ void stage_flush(const RefArgs &r, const float *buf, 
 // its last entry arrives.
 __device__ __forceinline__ void stage_put(const RefArgs &r, float *buf, int64_t first, int64_t x,
                                           float ds, float zh, int32_t src) {
-  const int e = (int)(x & 7);
+  const int e = (int)(x & (STAGE_N - 1));
   buf[e] = ds;
-  buf[8 + e] = zh;
-  reinterpret_cast<int32_t *>(buf + 16)[e] = src;
-  if (e == 7) stage_flush(r, buf, first, x + 1);
+  buf[STAGE_N + e] = zh;
+  reinterpret_cast<int32_t *>(buf + 2 * STAGE_N)[e] = src;
+  if (e == STAGE_N - 1) stage_flush(r, buf, first, x + 1);
 }
 
 // One 3D track over one 2D segment: the while loop of src/solver.c:409-524.
@@ -226,12 +231,12 @@ __device__ __forceinline__ int warp_incl_scan(int v, int lane) {
 constexpr int REF_KEEP = 4;
 
 // STAGED (pass 1): the warp's stacked rays keep their staging groups in
-// dynamic shared memory, 24 words per ray, Z rays per warp.
+// dynamic shared memory, STAGE_W words per ray, Z rays per warp.
 template <int PASS, bool STAGED = false>
 __global__ void __launch_bounds__(128) ref_expand(RefArgs r) {
   extern __shared__ float s_stage[];
   const int lane = threadIdx.x & 31;
-  float *wstage = STAGED ? s_stage + (size_t)(threadIdx.x >> 5) * r.Z * 24 : nullptr;
+  float *wstage = STAGED ? s_stage + (size_t)(threadIdx.x >> 5) * r.Z * STAGE_W : nullptr;
   const int64_t ij = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (ij >= r.n2d * r.P) return;        // uniform per warp
   const int64_t i = ij / r.P;
@@ -304,7 +309,7 @@ __global__ void __launch_bounds__(128) ref_expand(RefArgs r) {
           const int64_t t = ij * r.Z + k;
           const int64_t first = r.off[t], slot = first + cst[k];
           const int64_t seq = r.ij_base[ij] + local + (incl - cm);
-          float *stg = STAGED ? wstage + (size_t)k * 24 : nullptr;
+          float *stg = STAGED ? wstage + (size_t)k * STAGE_W : nullptr;
           if (c <= REF_KEEP) {
             for (int q = 0; q < c; ++q) {
               const int32_t src = sub_segment_source(r, seq + q);
@@ -346,7 +351,8 @@ __global__ void __launch_bounds__(128) ref_expand(RefArgs r) {
     __syncwarp();
     for (int k = lane; k < r.Z; k += 32) {
       const int64_t first = r.off[ij * r.Z + k], end = first + cst[k];
-      if (end > first && (end & 7) != 0) stage_flush(r, wstage + (size_t)k * 24, first, end);
+      if (end > first && (end & (STAGE_N - 1)) != 0)
+        stage_flush(r, wstage + (size_t)k * STAGE_W, first, end);
     }
   }
 }
@@ -649,8 +655,8 @@ int sweep_ref(int64_t *segments) {
   MOC_CUDA_TRY(cudaMemcpyAsync(r.d_ij_base, base.data(), sizeof(int64_t) * (size_t)pairs,
                                cudaMemcpyHostToDevice, st));
   MOC_CUDA_TRY(cudaMemcpyAsync(r.d_off + r.n3d, &M, sizeof(int64_t), cudaMemcpyHostToDevice, st));
-  // pass 1 with staged stores: one warp a block, 96 bytes of groups per ray
-  const size_t stage_bytes = (size_t)96 * r.Z;
+  // pass 1 with staged stores: one warp a block, STAGE_W words of groups per ray
+  const size_t stage_bytes = sizeof(float) * STAGE_W * (size_t)r.Z;
   if (stage_bytes <= (size_t)200 * 1024) {
     if (stage_bytes > 48 * 1024)
       MOC_CUDA_TRY(cudaFuncSetAttribute(ref_expand<1, true>,
