@@ -73,7 +73,7 @@ def _spec(**kw):
 SHAPES = [(32, 1), (32, 2), (32, 4), (16, 1), (16, 2), (8, 1), (8, 4), (4, 2), (10, 5), (10, 1)]
 
 
-@pytest.mark.parametrize("groups", [100, 7, 32, 20, 98, 40, 37])
+@pytest.mark.parametrize("groups", [100, 7, 32, 20, 98, 40, 37, 1, 2, 3])
 def test_plain_every_launch_shape_bit_exact(gpu_available, port, groups):
     import simplemoc_gb300 as sm
     spec = _spec(n_groups=groups, n_tracks_2d=16, z_stacked=10)
@@ -95,6 +95,34 @@ def test_plain_every_launch_shape_bit_exact(gpu_available, port, groups):
         assert rel_err(out["fine_flux"], st["fine_flux"]) <= PHI_TOL, (tpw, cpl)
         ran += 1
     assert ran >= 1
+
+
+@pytest.mark.parametrize("groups,axial_exp", [(100, 2), (7, 2), (3, 2), (40, 2), (10, 0)])
+def test_mixed_every_launch_shape_identical(gpu_available, groups, axial_exp):
+    """MIXED runs the same operations per group at every launch shape (groups in
+    packed pairs, a pair half-padded where G is odd), so psi is the same to the
+    bit at every shape that covers G."""
+    import simplemoc_gb300 as sm
+    spec = _spec(n_groups=groups, n_tracks_2d=16, z_stacked=10, axial_exp=axial_exp)
+    hp = sm.generate(spec)
+    ldg = (groups + 3) // 4 * 4
+    first = None
+    ran = 0
+    for tpw, cpl in SHAPES:
+        vw = 2 if (tpw, cpl) == (10, 5) else 4
+        if tpw * cpl * vw < ldg:
+            continue
+        with _solver(hp, mode="mixed") as s:
+            s.set_launch(tpw, cpl)
+            s.transport_sweep()
+            out = s.download(psi_f=True, fine_flux=True)
+        if first is None:
+            first = out
+        else:
+            assert np.array_equal(out["psi_f"], first["psi_f"]), (tpw, cpl)
+            assert rel_err(out["fine_flux"], first["fine_flux"]) <= PHI_TOL, (tpw, cpl)
+        ran += 1
+    assert ran >= 2
 
 
 STAGED_SHAPES = [(32, 1), (32, 2), (16, 1), (16, 2), (8, 1)]
