@@ -73,10 +73,15 @@ def _spec(**kw):
 SHAPES = [(32, 1), (32, 2), (32, 4), (16, 1), (16, 2), (8, 1), (8, 4), (4, 2), (10, 5), (10, 1)]
 
 
-@pytest.mark.parametrize("groups", [100, 7, 32, 20, 98, 40, 37, 1, 2, 3])
-def test_plain_every_launch_shape_bit_exact(gpu_available, port, groups):
+@pytest.mark.parametrize("groups,axial_exp", [(100, 2), (7, 2), (32, 2), (20, 2), (98, 2),
+                                              (40, 2), (37, 2), (1, 2), (2, 2), (3, 2),
+                                              (100, 0), (37, 0), (3, 0)])
+def test_plain_every_launch_shape_bit_exact(gpu_available, port, groups, axial_exp):
+    """PLAIN psi equals the oracle's to the bit at every launch shape that covers
+    G, quadratic and flat source, G from 1 to 100 (pairs of groups, half-padded
+    where G is odd)."""
     import simplemoc_gb300 as sm
-    spec = _spec(n_groups=groups, n_tracks_2d=16, z_stacked=10)
+    spec = _spec(n_groups=groups, n_tracks_2d=16, z_stacked=10, axial_exp=axial_exp)
     hp = sm.generate(spec)
     st = oracle.fresh_state(hp)
     op = oracle.make_problem(hp)
