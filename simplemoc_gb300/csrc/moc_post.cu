@@ -105,13 +105,37 @@ __global__ void __launch_bounds__(RTHREADS) renorm_partials(const T *__restrict_
   if (threadIdx.x == 0) partials[blockIdx.x] = b;
 }
 
-// step 2: total, norm factor (src/solver.c:1203: float norm_factor = 1.0 / total)
+// The sum of n partials by one warp, in a fixed order: lane l adds partials
+// l, l + 32, l + 64, ... into four accumulators in turn, and the lanes' sums
+// meet in a fixed shuffle tree.  The order never depends on timing, so every
+// run gives the same bits; a single thread adding 1024 partials one after the
+// other took ~60-160 us a call, which the batched iteration pays once per core.
+// Returns the sum in lane 0.
+__device__ __forceinline__ double warp_fixed_sum(const double *__restrict__ x, int n) {
+  const int lane = threadIdx.x & 31;
+  double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+  int i = lane;
+  for (; i + 96 < n; i += 128) {
+    s0 += x[i];
+    s1 += x[i + 32];
+    s2 += x[i + 64];
+    s3 += x[i + 96];
+  }
+  for (; i < n; i += 32) s0 += x[i];
+  double s = (s0 + s1) + (s2 + s3);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+  return s;
+}
+
+// step 2: total, norm factor (src/solver.c:1203: float norm_factor = 1.0 / total).
+// One warp (launched with 32 threads).
 template <typename T>
 __global__ void renorm_finalize(const double *__restrict__ partials, int nparts,
                                 double *__restrict__ scalars) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  double total = 0.0;
-  for (int i = 0; i < nparts; ++i) total += partials[i];
+  if (blockIdx.x != 0 || threadIdx.x >= 32) return;
+  const double total = warp_fixed_sum(partials, nparts);
+  if (threadIdx.x != 0) return;
   scalars[SC_TOTAL_FISSION] = total;
   if (sizeof(T) == 4)
     scalars[SC_NORM] = (double)(float)(1.0 / total);
@@ -259,20 +283,16 @@ __global__ void __launch_bounds__(RTHREADS) keff_partials(const T *__restrict__ 
   if (threadIdx.x == 0) partials[2 * RBLOCKS + blockIdx.x] = f;
 }
 
+// One warp (launched with 32 threads).
 __global__ void update_finalize(const double *__restrict__ partials, double *__restrict__ scalars,
                                 int with_residual, int with_keff) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  if (with_residual) {
-    double r = 0.0;
-    for (int i = 0; i < RBLOCKS; ++i) r += partials[i];
-    scalars[SC_RESIDUAL] = r;
-  }
+  if (blockIdx.x != 0 || threadIdx.x >= 32) return;
+  const double r = with_residual ? warp_fixed_sum(partials, RBLOCKS) : 0.0;
+  const double a = with_keff ? warp_fixed_sum(partials + RBLOCKS, RBLOCKS) : 0.0;
+  const double f = with_keff ? warp_fixed_sum(partials + 2 * RBLOCKS, RBLOCKS) : 0.0;
+  if (threadIdx.x != 0) return;
+  if (with_residual) scalars[SC_RESIDUAL] = r;
   if (with_keff) {
-    double a = 0.0, f = 0.0;
-    for (int i = 0; i < RBLOCKS; ++i) {
-      a += partials[RBLOCKS + i];
-      f += partials[2 * RBLOCKS + i];
-    }
     scalars[SC_ABS] = a;
     scalars[SC_FISSION] = f;
     const double k = f / (a + scalars[SC_LEAKAGE]);
